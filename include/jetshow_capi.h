@@ -1,0 +1,367 @@
+/*
+ * jetshow_capi.h -- C ABI of the GB300 (sm_103a) renderer for jetshow's
+ * per-pixel polarised synchrotron transfer path:
+ *
+ *     ray -> geometry hit -> tau pass -> I / IQUV pass -> pixel value
+ *
+ * Plain C types only (no CUDA, no C++ and no torch types), so that a ctypes,
+ * cgo, JNI or pybind11 binding can bind it directly.  Every entry point that
+ * can fail returns an int status (JSH_OK == 0, negative on error) and leaves
+ * a message retrievable with jsh_last_error().
+ *
+ * Reference interfaces replaced (paths inside the jetshow project):
+ *   - Observation::run / observe_single_pixel / getImage
+ *       src/Observation.cpp:20-41, src/Observation.cpp:349-395,
+ *       include/Observation.h:12-24                -> jsh_observation_run
+ *   - ImagePlane / Image / Ray construction
+ *       src/ImagePlane.cpp:11-33, src/Image.cpp:44-194,
+ *       include/logspace.h:25-33, src/Ray.cpp:9-20 -> jsh_plane_rays
+ *   - BaseGeometry::hit family
+ *       src/Cone.cpp:56-118, src/Cylinder.cpp:35-95,
+ *       src/Parabaloid.cpp:39-60, src/ParabaloidCone.cpp:45-94
+ *                                                   -> jsh_trace_plane, jsh_hit_rays
+ *   - pyjetshow.get_i_image (pybind11)
+ *       src/pyjetshow.cpp:69-173, :181-201         -> jsh_mas_to_pc +
+ *                                                      jsh_observation_run
+ *   - SimulationInterpolater / create_triangulation
+ *       src/SimulationInterpolater.cpp:30-117      -> jsh_grid_triangulate,
+ *                                                      jsh_grid_upload,
+ *                                                      jsh_grid_interpolate
+ *   - comoving_transfer_distance2 / mas_to_pc
+ *       src/utils.cpp:186-208                       -> jsh_mas_to_pc
+ *
+ * Units follow the reference: lengths in cm, magnetic field in G, densities
+ * in cm^-3, frequencies in Hz, angles in rad.  Images are row-major
+ * [n_nu][n_across][n_along] doubles, the layout of Image::getImage
+ * (src/Image.cpp:16-28) with a leading frequency axis.
+ */
+#ifndef JETSHOW_CAPI_H
+#define JETSHOW_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JSH_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- status */
+#define JSH_OK 0
+#define JSH_ERR_INVALID (-1)  /* bad argument or descriptor              */
+#define JSH_ERR_CUDA (-2)     /* CUDA runtime error                      */
+#define JSH_ERR_OOM (-3)      /* request exceeds the context HBM budget  */
+#define JSH_ERR_TIMEOUT (-4)  /* wait timed out                          */
+#define JSH_ERR_NOT_FOUND (-5)/* unknown request / grid id               */
+#define JSH_ERR_NO_DEVICE (-6)/* no CUDA device or wrong architecture    */
+#define JSH_ERR_CANCELLED (-7)/* request cancelled before it ran         */
+
+/* Per (frequency, pixel) status bits written to jsh_image.status. */
+#define JSH_ST_HIT 0x1u            /* the pixel's ray intersects the jet          */
+#define JSH_ST_TAU_CROSSED 0x2u    /* tau reached tau_max; path truncated there    */
+#define JSH_ST_STEP_LIMIT 0x4u     /* a segment needed more than max_steps steps   */
+#define JSH_ST_FAIL_LIMIT 0x8u     /* 500 consecutive rejected steps               */
+#define JSH_ST_BISECT_LIMIT 0x10u  /* tau_max crossing bisection did not converge  */
+#define JSH_ST_NAN 0x20u           /* NaN/Inf met in the state or step size        */
+#define JSH_ST_UB_GEOMETRY 0x40u   /* reference behaviour undefined; treated as miss */
+#define JSH_ST_DT_UNDERFLOW 0x80u  /* the step no longer advances the time        */
+#define JSH_ST_IQUV 0x100u         /* the I/IQUV pass ran (tau > tau_min)          */
+
+/* ------------------------------------------------------------ geometry */
+enum jsh_geometry_kind {
+  JSH_GEO_CONE = 1,            /* Cone(origin, direction, angle, big_scale)        */
+  JSH_GEO_CYLINDER = 2,        /* Cylinder(origin, direction, r)                   */
+  JSH_GEO_PARABALOID = 3,      /* Parabaloid(origin, direction, r0, big_scale)     */
+  JSH_GEO_PARABALOID_CONE = 4  /* ParabaloidCone(origin, direction, r0, z0, scale) */
+};
+
+typedef struct jsh_geometry_desc {
+  int32_t kind;        /* enum jsh_geometry_kind */
+  int32_t reserved;
+  double origin[3];    /* [cm] */
+  double direction[3]; /* normalised by the library, as the constructors do */
+  double angle;        /* cone half-opening angle [rad] */
+  double big_scale;    /* [cm] length of (half-)infinite paths (cone, paraboloid) */
+  double r;            /* cylinder radius [cm] */
+  double r0;           /* paraboloid radius at z = 1 pc [cm] */
+  double z0;           /* ParabaloidCone break [cm] */
+} jsh_geometry_desc;
+
+/* ---------------------------------------------------------------- fields */
+enum jsh_bfield_kind {
+  /* scalar ("tangled") fields, src/BField.cpp:35-64 */
+  JSH_B_RANDOM_SCALAR = 1,          /* p = {b0, m}:  b0 (|x|/pc)^-m              */
+  JSH_B_RANDOM_SCALAR_Z = 2,        /* p = {b0, m}:  b0 (|z|/pc)^-m              */
+  JSH_B_COMPOSITE_RANDOM_SCALAR_Z = 3, /* p = {b0, m_inner, m_outer, z0}          */
+  /* vector fields, src/BField.cpp:67-146, :196-207 */
+  JSH_B_CONST_CYLINDER = 10,        /* p = {b0, n}                               */
+  JSH_B_CONST_CYLINDER_Z = 11,      /* p = {b0, n}                               */
+  JSH_B_RADIAL_CONICAL = 12,        /* p = {b0, n}                               */
+  JSH_B_TOROIDAL = 13,              /* p = {b0, n}    (phi = atan(y/x))          */
+  JSH_B_HELICAL_CYLINDER = 14,      /* p = {b0, pitch}                           */
+  JSH_B_SPIRAL_CONICAL = 15,        /* p = {b0, pitch}                           */
+  JSH_B_FORCE_FREE_CYLINDRICAL = 16,/* p = {b0, mu}                              */
+  /* builder-defined helical field of a conical jet (no reference class):
+   * B = b0 (|x|/pc)^-n (sin(pitch) phi_hat + cos(pitch) z_hat),
+   * phi_hat = (-y, x, 0)/hypot(x, y); p = {b0, n, pitch, atan_quirk}.
+   * atan_quirk != 0 reproduces phi = atan(y/x) of ToroidalBField, i.e.
+   * phi_hat flips sign for x < 0. */
+  JSH_B_HELICAL_CONICAL = 17,
+  /* gridded: p = {grid id, field index of B_p, field index of B_phi} */
+  JSH_B_SIMULATION = 20
+};
+
+enum jsh_nfield_kind {
+  JSH_N_CONST = 1,             /* p = {n}                                       */
+  JSH_N_BK = 2,                /* p = {n0, n}:  n0 (|x|/pc)^-n                  */
+  JSH_N_BKZ = 3,               /* p = {n0, n}:  n0 (|z|/pc)^-n                  */
+  JSH_N_COMPOSITE_BK = 4,      /* p = {n0, n_inner, n_outer, z0}                */
+  JSH_N_SIMULATION = 20        /* p = {grid id, field index}                    */
+};
+
+enum jsh_vfield_kind {
+  JSH_V_CONST_FLAT = 1,              /* p = {Gamma}                              */
+  JSH_V_SHEARED_FLAT = 2,            /* p = {Gamma_axis, Gamma_border, r}        */
+  JSH_V_SHEATH_FLAT = 3,             /* p = {Gamma_spine, Gamma_sheath, r_sheath}*/
+  JSH_V_CONST_CENTRAL = 4,           /* p = {Gamma, ox, oy, oz}                  */
+  JSH_V_SHEARED_CENTRAL = 5,         /* p = {Gamma_axis, Gamma_border, theta, ox, oy, oz} */
+  JSH_V_SHEATH_CENTRAL = 6,          /* p = {Gamma_spine, Gamma_sheath, theta_sheath, ox, oy, oz} */
+  JSH_V_CONST_PARABOLIC = 7,         /* p = {Gamma, Rz0}                         */
+  JSH_V_ACC_PARABOLIC = 8,           /* p = {Gamma0, R0, Rz0}                    */
+  JSH_V_SHEARED_ACC_PARABOLIC = 9,   /* p = {Gamma_axis0, Gamma_border0, R0, Rz0}*/
+  JSH_V_ACC_PARABOLIC_CONST_CONE = 10,         /* p = {Gamma0, Rz0, z0}          */
+  JSH_V_SHEARED_ACC_PARABOLIC_CONST_CONE = 11, /* p = {Gamma_axis0, Gamma_border0, Rz0, z0} */
+  JSH_V_SIMULATION = 20              /* p = {grid id, field index of Gamma}      */
+};
+
+typedef struct jsh_field_desc {
+  int32_t kind;            /* one of the enums above */
+  int32_t in_plasma_frame; /* vector B and N: 1 = given in the plasma frame */
+  double p[8];             /* kind-specific parameters, see the enums */
+} jsh_field_desc;
+
+typedef struct jsh_model_desc {
+  jsh_geometry_desc geometry;
+  jsh_field_desc bfield;
+  jsh_field_desc nfield;
+  jsh_field_desc vfield;
+  double s;                /* power-law index in the coefficients
+                              (the reference hard-codes s = 3.42, src/Jet.cpp:32) */
+  double gamma_min;        /* low-energy cut-off in k_F_r, k_C_r (src/utils.cpp:86-98) */
+  double thermal_fraction; /* n_th / n for cold-plasma k_F_c, k_C_c terms (builder-defined) */
+} jsh_model_desc;
+
+/* ----------------------------------------------------------- image plane */
+typedef struct jsh_plane_desc {
+  uint64_t n_across;          /* image_size.first; must be even */
+  uint64_t n_along;           /* image_size.second */
+  double lg_pixel_size_start_cm;
+  double lg_pixel_size_stop_cm;
+  double los_angle;           /* [rad] */
+} jsh_plane_desc;
+
+/* ----------------------------------------------------------- parameters */
+enum jsh_output { JSH_OUT_I = 1, JSH_OUT_FULL = 2 };
+enum jsh_precision {
+  JSH_PREC_FP64 = 1,  /* every operation in FP64 (the plain GPU drop-in)        */
+  JSH_PREC_MIXED = 2  /* FP32 RHS and RK stages; FP64 tau, Faraday angle, t,
+                         step-size control and error norm                       */
+};
+enum jsh_schedule {
+  JSH_SCHED_STATIC = 1,     /* one thread per (ray, frequency) for its lifetime */
+  JSH_SCHED_PERSISTENT = 2  /* persistent CTAs, global work queue, lanes refilled
+                               from the queue as their rays finish              */
+};
+
+typedef struct jsh_params {
+  int32_t n;               /* initial step = L / n (reference n = 100)              */
+  int32_t output;          /* enum jsh_output                                       */
+  int32_t precision;       /* enum jsh_precision                                    */
+  int32_t schedule;        /* enum jsh_schedule                                     */
+  double tau_max;          /* stop the tau pass at tau >= tau_max (reference 1e4)   */
+  double tau_min;          /* run the I pass only if tau > tau_min (1e-10)          */
+  double dt_max;           /* [cm] largest tau-pass step, 0 = no limit              */
+  double tau_atol;         /* tau pass tolerances (reference 1e-7, 1e-14)           */
+  double tau_rtol;
+  double atol;             /* I / IQUV pass tolerances (reference 1e-9, 1e-9)        */
+  double rtol;
+  double tau_precision;    /* |tau - tau_max| target of the crossing bisection (1)   */
+  int64_t max_steps;       /* accepted+rejected steps per segment and pass (0: 1<<22)*/
+  int32_t block_size;      /* 0 = autotuned / default                               */
+  int32_t refill_threshold;/* persistent schedule: refill when this many lanes idle  */
+  int32_t ctas_per_sm;     /* persistent schedule: 0 = occupancy maximum             */
+  int32_t reserved;
+} jsh_params;
+
+/* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
+ * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,
+ * dt_max = 0, tau tolerances (1e-7, 1e-14), I tolerances (1e-9, 1e-9),
+ * tau_precision = 1, output I, FP64, static schedule. */
+void jsh_params_default(jsh_params* p);
+
+/* --------------------------------------------------------------- outputs */
+typedef struct jsh_image {
+  /* Each non-NULL plane holds n_nu * n_across * n_along values. */
+  double* tau;
+  double* l;      /* untruncated path length through the jet [cm] */
+  double* I;
+  double* Q;
+  double* U;
+  double* V;
+  uint32_t* status;
+} jsh_image;
+
+typedef struct jsh_stats {
+  uint64_t n_pixels;
+  uint64_t n_hit_pixels;    /* pixels whose ray intersects the geometry  */
+  uint64_t n_work_items;    /* hit pixels x frequencies                   */
+  uint64_t rhs_evals;       /* right-hand-side evaluations on the device  */
+  uint64_t steps_accepted;
+  uint64_t steps_rejected;
+  uint32_t status_or;       /* OR of all per-item status bits             */
+  uint32_t kernels_launched;
+  double device_ms;         /* CUDA-event time of the render kernels      */
+  double total_ms;          /* host wall time of the call                 */
+} jsh_stats;
+
+/* ------------------------------------------------------------- context */
+typedef struct jsh_ctx jsh_ctx;
+
+int jsh_abi_version(void);
+const char* jsh_last_error(void); /* thread-local message of the last failure */
+
+/* Create a context on CUDA device `device`.  hbm_budget_bytes caps the device
+ * memory the context may hold for requests (0 = 80% of free memory). */
+int jsh_ctx_create(int device, uint64_t hbm_budget_bytes, jsh_ctx** out);
+void jsh_ctx_destroy(jsh_ctx* ctx);
+
+/* Observation::run + getImage for n_nu frequencies in one call, host buffers
+ * in and out (host<->device copies included).  nu_hz are source-frame
+ * frequencies (the reference multiplies by 1e9 (1+z) before the call). */
+int jsh_observation_run(jsh_ctx* ctx, const jsh_model_desc* model,
+                        const jsh_plane_desc* plane, const double* nu_hz,
+                        int32_t n_nu, const jsh_params* params,
+                        jsh_image* host_out, jsh_stats* stats);
+
+/* Same, but the outputs are DEVICE pointers and the work is enqueued on
+ * `cuda_stream` (a cudaStream_t, NULL = legacy default stream).  The call
+ * returns after enqueueing; the caller synchronises the stream. */
+int jsh_observation_run_device(jsh_ctx* ctx, const jsh_model_desc* model,
+                               const jsh_plane_desc* plane, const double* nu_hz,
+                               int32_t n_nu, const jsh_params* params,
+                               void* cuda_stream, jsh_image* device_out);
+
+/* Device counters of the last jsh_observation_run_device call on this
+ * context (synchronises the context's work first). */
+int jsh_last_stats(jsh_ctx* ctx, jsh_stats* stats);
+
+/* Ray generation on the device (ImagePlane + Image + Ray ctors): origins
+ * [n_across*n_along][3], the common unit direction [3], pixel sizes
+ * [n_across*n_along] (cm), all host buffers (any may be NULL). */
+int jsh_plane_rays(jsh_ctx* ctx, const jsh_plane_desc* plane, double* origins,
+                   double* direction, double* pixel_sizes);
+
+/* Geometry hit of every pixel's ray on the device.  n_seg[pix] in {0,1,2};
+ * seg[pix][k] = {point_in xyz, point_out xyz} (k < 2), host buffers. */
+int jsh_trace_plane(jsh_ctx* ctx, const jsh_model_desc* model,
+                    const jsh_plane_desc* plane, int32_t* n_seg, double* seg,
+                    uint32_t* status);
+
+/* Geometry hit of arbitrary rays (origins[n][3], directions[n][3], the
+ * directions are normalised like Ray::Ray).  Same outputs as above. */
+int jsh_hit_rays(jsh_ctx* ctx, const jsh_model_desc* model, const double* origins,
+                 const double* directions, int64_t n, int32_t* n_seg,
+                 double* seg, uint32_t* status);
+
+/* --------------------------------------------------------- cosmology */
+typedef struct jsh_cosmology {
+  double H0;       /* km/s/Mpc (reference default 69.32)          */
+  double omega_M;  /* (0.2865)                                    */
+  double omega_V;  /* (0.7134130719051658)                        */
+  double gamma_nu; /* (8.69280948342326e-05)                      */
+} jsh_cosmology;
+
+/* Parsecs per milliarcsecond at redshift z (mas_to_pc, src/utils.cpp:205-208).
+ * cosmo == NULL selects the reference defaults. */
+double jsh_mas_to_pc(double z, const jsh_cosmology* cosmo);
+
+/* --------------------------------------------------------- gridded fields */
+/* Delaunay triangulation of n points (xy[n][2]) on the host.  tri_out must
+ * hold 3*(2n) int32; *n_tri receives the triangle count. */
+int jsh_grid_triangulate(const double* xy, int64_t n, int32_t* tri_out,
+                         int64_t* n_tri);
+
+/* Upload a triangulated (z, r) grid once: xy[n][2] in pc (z, r), values
+ * [n][n_fields] FP32, tri[n_tri][3].  Returns a grid id for field
+ * descriptors (JSH_*_SIMULATION). */
+int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n_points,
+                    const float* values, int32_t n_fields, const int32_t* tri,
+                    int64_t n_tri, int32_t* grid_id);
+
+/* Interpolate field `field` of a grid at host points (z, r) in pc on the
+ * device (SimulationInterpolater::interpolated_value).  out[n]. */
+int jsh_grid_interpolate(jsh_ctx* ctx, int32_t grid_id, int32_t field,
+                         const double* zr, int64_t n, double nan_value,
+                         double* out);
+
+/* --------------------------------------------------------- serving */
+typedef struct jsh_server jsh_server;
+typedef uint64_t jsh_request_id;
+
+typedef struct jsh_server_config {
+  int32_t max_inflight_batches; /* concurrent device batches (streams), >= 1 */
+  int32_t max_batch_requests;   /* requests merged into one device batch      */
+  int32_t precision;            /* enum jsh_precision for every request       */
+  int32_t use_graphs;           /* capture each batch's launch sequence       */
+  uint64_t hbm_budget_bytes;    /* device memory the queue may hold (0: ctx)  */
+} jsh_server_config;
+
+typedef struct jsh_request_stats {
+  double queue_ms;    /* submit -> admitted                               */
+  double service_ms;  /* admitted -> result on host                       */
+  double latency_ms;  /* submit -> result on host                         */
+  uint64_t n_work_items;
+  uint32_t status_or;
+  int32_t batch_size; /* requests in the device batch this one ran in     */
+} jsh_request_stats;
+
+int jsh_server_create(jsh_ctx* ctx, const jsh_server_config* cfg,
+                      jsh_server** out);
+void jsh_server_destroy(jsh_server* srv);
+/* Enqueue a render; copies every descriptor and nu_hz.  Never blocks on the
+ * device.  JSH_ERR_OOM if the request alone exceeds the HBM budget. */
+int jsh_server_submit(jsh_server* srv, const jsh_model_desc* model,
+                      const jsh_plane_desc* plane, const double* nu_hz,
+                      int32_t n_nu, const jsh_params* params,
+                      jsh_request_id* id);
+/* 1 if finished, 0 if not yet, negative on error. */
+int jsh_server_poll(jsh_server* srv, jsh_request_id id);
+/* Wait up to timeout_ms (< 0: forever) and copy the result planes into
+ * host_out (planes may be NULL); releases the request. */
+int jsh_server_wait(jsh_server* srv, jsh_request_id id, int32_t timeout_ms,
+                    jsh_image* host_out, jsh_request_stats* stats);
+/* Cancel a request that has not been admitted yet. */
+int jsh_server_cancel(jsh_server* srv, jsh_request_id id);
+
+/* --------------------------------------------------------- autotuning */
+typedef struct jsh_tuning {
+  int32_t block_size;
+  int32_t ctas_per_sm;
+  int32_t refill_threshold;
+  int32_t reserved;
+  double ms;            /* best measured time */
+} jsh_tuning;
+
+/* Time the persistent schedule over a grid of block sizes, CTAs per SM and
+ * refill thresholds on this request and store the fastest in the context;
+ * later requests with block_size == 0 use it. */
+int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model,
+                 const jsh_plane_desc* plane, const double* nu_hz,
+                 int32_t n_nu, const jsh_params* params, jsh_tuning* best);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JETSHOW_CAPI_H */

@@ -1,0 +1,68 @@
+// jsh_context.h -- the context behind the C ABI: device, streams, the
+// workspace arena of the blocking entry points, uploaded grids, tuning.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <mutex>
+#include <vector>
+
+#include "jsh_launch.h"
+
+#define JSH_CUDA_TRY(expr)                                                              \
+  do {                                                                                  \
+    cudaError_t e_ = (expr);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      jsh_set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return JSH_ERR_CUDA;                                                              \
+    }                                                                                   \
+  } while (0)
+
+struct JshGridSlot {
+  bool used = false;
+  JshGrid view{};
+  void* mem = nullptr;  // one allocation holding every array of the grid
+  size_t bytes = 0;
+};
+
+// Layout of one request's device memory inside an arena allocation.
+struct JshRequestLayout {
+  size_t off_req, off_counters, off_nhit, off_queue, off_nu, off_along_size, off_along_center, off_across,
+      off_hits, off_out[7];
+  size_t total;
+  bool own_outputs;
+};
+
+struct jsh_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ws_ready = nullptr;
+  std::mutex mu;
+  uint64_t budget = 0;
+  std::atomic<uint64_t> used{0};
+  void* ws = nullptr;  // workspace of the blocking / device entry points
+  size_t ws_cap = 0;
+  JshRequest* h_req = nullptr;               // pinned staging of one request
+  unsigned long long* h_counters = nullptr;  // pinned [8]
+  JshGridSlot grids[JSH_MAX_GRIDS];
+  bool tuned = false;
+  JshLaunchShape shape{128, 0, 8};
+  jsh_stats last{};
+  bool last_pending = false;
+  size_t last_counters_off = 0, last_nhit_off = 0;
+  uint64_t last_npix = 0;
+  int last_n_nu = 0;
+};
+
+// Helpers shared by the C-ABI translation units.
+int jsh_prepare_request(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_desc* plane,
+                        const jsh_params* params, int32_t n_nu, JshRequest* req, uint64_t* npix);
+void jsh_request_layout(uint64_t npix, uint64_t n_along, uint64_t n_across, int32_t n_nu, bool own_outputs,
+                        JshRequestLayout* L);
+void jsh_bind_request(JshRequest* req, char* base, const JshRequestLayout& L, bool own_outputs);
+int jsh_alloc_device(jsh_ctx* ctx, size_t bytes, void** p);
+void jsh_free_device(jsh_ctx* ctx, void* p, size_t bytes);
+JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params);
+void jsh_set_error(const char* fmt, ...);

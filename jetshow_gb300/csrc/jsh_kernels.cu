@@ -1,0 +1,317 @@
+// jsh_kernels.cu -- ray generation, hit/compaction and the static-schedule
+// FP64 transfer kernels, plus their launchers.  The mixed-precision and
+// persistent kernels are in jsh_persistent.cu.
+#include <cuda_runtime.h>
+
+#include "jsh_launch.h"
+#include "jsh_transfer64.cuh"
+
+using namespace jsh;
+
+namespace {
+
+constexpr int kPlaneThreads = 128;
+constexpr int kHitThreads = 256;
+
+// ---------------------------------------------------------------- plane
+// pyLogspace by repeated multiplication and the running partial sum are
+// sequential recurrences (include/logspace.h:9-33, src/Image.cpp:70-75): one
+// thread per request walks them so every value rounds as in the reference.
+__global__ void plane_along_kernel(const JshRequest* __restrict__ reqs) {
+  if (threadIdx.x != 0) return;
+  const JshPlane& p = reqs[blockIdx.x].plane;
+  double cur = p.real_start, acc = 0.0;
+  for (uint64_t j = 0; j < p.n_along; ++j) {
+    p.along_size[j] = cur;
+    acc = (j == 0) ? cur : ad(acc, cur);
+    p.along_center[j] = sb(acc, ml(0.5, cur));
+    cur = ml(cur, p.real_base);
+  }
+}
+
+// Column j of the across table: partial sums of n_across/2 copies of the
+// column's pixel size, minus half a size (src/Image.cpp:110-126).
+__global__ void plane_across_kernel(const JshRequest* __restrict__ reqs) {
+  const JshPlane& p = reqs[blockIdx.y].plane;
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.n_along) return;
+  uint64_t nh = p.n_across / 2, na = p.n_along;
+  double s = ml(p.along_size[j], 1.0);
+  double half = ml(0.5, s);
+  double a = 0.0;
+  for (uint64_t k = 0; k < nh; ++k) {
+    a = (k == 0) ? s : ad(a, s);
+    p.across_pos[k * na + j] = sb(a, half);
+  }
+}
+
+// ------------------------------------------------------------------ hit
+__global__ void hit_kernel(const JshRequest* __restrict__ reqs) {
+  const JshRequest& R = reqs[blockIdx.y];
+  const JshPlane& p = R.plane;
+  uint64_t pix = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool valid = pix < R.npix;
+  Hits h;
+  h.n = 0;
+  h.status = 0;
+  if (valid) {
+    V3 ro = plane_origin(p, pix / p.n_along, pix % p.n_along);
+    geo_hit(R.model, ro, mk(p.dx, p.dy, p.dz), h);
+  }
+  bool hit = valid && h.n > 0;
+  unsigned mask = __ballot_sync(0xffffffffu, hit);
+  int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (mask) {
+    int leader = __ffs(mask) - 1;
+    if (lane == leader) base = atomicAdd(R.n_hit, (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+  }
+  if (hit) {
+    unsigned slot = base + __popc(mask & ((1u << lane) - 1u));
+    JshHit& H = R.hits[slot];
+    H.pix = (int64_t)pix;
+    H.nseg = h.n;
+    H.status = (int32_t)h.status;
+#pragma unroll
+    for (int s = 0; s < JSH_MAX_SEG; ++s) {
+      const Seg& S = h.s[s < h.n ? s : 0];
+      H.seg[s][0] = S.in.x;
+      H.seg[s][1] = S.in.y;
+      H.seg[s][2] = S.in.z;
+      H.seg[s][3] = S.out.x;
+      H.seg[s][4] = S.out.y;
+      H.seg[s][5] = S.out.z;
+    }
+  } else if (valid) {
+    for (int f = 0; f < R.n_nu; ++f) {
+      uint64_t q = (uint64_t)f * R.npix + pix;
+      if (R.tau) R.tau[q] = 0.0;
+      if (R.l) R.l[q] = 0.0;
+      if (R.I) R.I[q] = 0.0;
+      if (R.Q) R.Q[q] = 0.0;
+      if (R.U) R.U[q] = 0.0;
+      if (R.V) R.V[q] = 0.0;
+      if (R.status) R.status[q] = h.status;
+    }
+  }
+}
+
+__global__ void hit_rays_kernel(JshModel m, const double* __restrict__ orig, const double* __restrict__ dir,
+                                int64_t n, int32_t* nseg, double* seg, uint32_t* status) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  V3 ro = mk(orig[3 * i], orig[3 * i + 1], orig[3 * i + 2]);
+  V3 rd = vnormalize(mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]));
+  Hits h;
+  h.n = 0;
+  h.status = 0;
+  geo_hit(m, ro, rd, h);
+  if (nseg) nseg[i] = h.n;
+  if (status) status[i] = h.status | (h.n ? JSH_ST_HIT : 0u);
+  if (seg) {
+    for (int s = 0; s < JSH_MAX_SEG; ++s) {
+      double* o = seg + 12 * i + 6 * s;
+      if (s < h.n) {
+        o[0] = h.s[s].in.x;
+        o[1] = h.s[s].in.y;
+        o[2] = h.s[s].in.z;
+        o[3] = h.s[s].out.x;
+        o[4] = h.s[s].out.y;
+        o[5] = h.s[s].out.z;
+      } else {
+        for (int q = 0; q < 6; ++q) o[q] = 0.0;
+      }
+    }
+  }
+}
+
+__global__ void plane_rays_kernel(JshPlane p, double* orig, double* sizes) {
+  uint64_t pix = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t npix = p.n_across * p.n_along;
+  if (pix >= npix) return;
+  uint64_t i = pix / p.n_along, j = pix % p.n_along;
+  if (orig) {
+    V3 o = plane_origin(p, i, j);
+    orig[3 * pix] = o.x;
+    orig[3 * pix + 1] = o.y;
+    orig[3 * pix + 2] = o.z;
+  }
+  if (sizes) sizes[pix] = p.along_size[j];
+}
+
+__global__ void grid_interp_kernel(JshGrid G, int field, const double* zr, int64_t n, double nan_value,
+                                   double* out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = grid_value(G, field, zr[2 * i], zr[2 * i + 1], nan_value);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ transfer
+namespace jsh {
+
+// Exclusive prefix of work items (n_hit * n_nu) over the batch, in shared memory.
+__device__ __forceinline__ void batch_prefix(const JshRequest* __restrict__ reqs, int n_req,
+                                             unsigned long long* base) {
+  if (threadIdx.x == 0) {
+    unsigned long long acc = 0;
+    for (int r = 0; r < n_req; ++r) {
+      base[r] = acc;
+      acc += (unsigned long long)(*reqs[r].n_hit) * (unsigned long long)reqs[r].n_nu;
+    }
+    base[n_req] = acc;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int find_request(const unsigned long long* base, int n_req, unsigned long long w) {
+  int lo = 0, hi = n_req - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (base[mid] <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Per-request device counters: warp-aggregated when the whole warp works on
+// one request, per-lane otherwise.
+__device__ __forceinline__ void add_counters(const JshRequest* __restrict__ reqs, int r, bool active,
+                                             unsigned long long evals, unsigned long long acc,
+                                             unsigned long long rej, unsigned status) {
+  int r0 = __shfl_sync(0xffffffffu, r, 0);
+  bool same = __all_sync(0xffffffffu, !active || r == r0);
+  bool any = __any_sync(0xffffffffu, active);
+  if (!any) return;
+  if (same) {
+    unsigned long long e = warp_sum(active ? evals : 0), a = warp_sum(active ? acc : 0),
+                       j = warp_sum(active ? rej : 0);
+    unsigned st = __reduce_or_sync(0xffffffffu, active ? status : 0u);
+    if ((threadIdx.x & 31) == 0) {
+      unsigned long long* c = reqs[r0].counters;
+      atomicAdd(&c[0], e);
+      atomicAdd(&c[1], a);
+      atomicAdd(&c[2], j);
+      atomicOr(&c[3], (unsigned long long)st);
+    }
+  } else if (active) {
+    unsigned long long* c = reqs[r].counters;
+    atomicAdd(&c[0], evals);
+    atomicAdd(&c[1], acc);
+    atomicAdd(&c[2], rej);
+    atomicOr(&c[3], (unsigned long long)status);
+  }
+}
+
+__device__ __forceinline__ void write_item(const JshRequest& R, int f, int64_t pix, const ItemOut& o) {
+  uint64_t q = (uint64_t)f * R.npix + (uint64_t)pix;
+  if (R.tau) R.tau[q] = o.tau;
+  if (R.l) R.l[q] = o.l;
+  if (R.I) R.I[q] = o.iquv[0];
+  if (R.Q) R.Q[q] = o.iquv[1];
+  if (R.U) R.U[q] = o.iquv[2];
+  if (R.V) R.V[q] = o.iquv[3];
+  if (R.status) R.status[q] = o.status;
+}
+
+}  // namespace jsh
+
+namespace {
+
+// One thread per (request, hit ray, frequency), all FP64.  Items are laid
+// out frequency-major within a request so adjacent lanes trace adjacent
+// pixels (similar path lengths, less divergence).
+__global__ void __launch_bounds__(128) transfer_static64_kernel(const JshRequest* __restrict__ reqs, int n_req) {
+  __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
+  batch_prefix(reqs, n_req, base);
+  unsigned long long w = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool active = w < base[n_req];
+  int r = 0;
+  Ctl64 tot{0, 0, 0, 0, 0, 0, 0};
+  ItemOut o;
+  o.status = 0;
+  if (active) {
+    r = find_request(base, n_req, w);
+    const JshRequest& R = reqs[r];
+    unsigned long long local = w - base[r];
+    unsigned nhit = *R.n_hit;
+    int f = (int)(local / nhit);
+    unsigned h = (unsigned)(local % nhit);
+    const JshHit& H = R.hits[h];
+    if (R.P.full) transfer_item64<true>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
+    else transfer_item64<false>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
+    write_item(R, f, H.pix, o);
+  }
+  add_counters(reqs, r, active, tot.evals, tot.acc, tot.rej, o.status);
+}
+
+}  // namespace
+
+// Defined in jsh_persistent.cu.
+cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int schedule, bool full,
+                                      uint64_t max_items, const JshLaunchShape& shape, unsigned int* queue,
+                                      int num_sms, cudaStream_t stream);
+cudaError_t jsh_launch_transfer_persistent64(const JshRequest* d_reqs, int n_req, uint64_t max_items,
+                                             const JshLaunchShape& shape, unsigned int* queue, int num_sms,
+                                             cudaStream_t stream);
+
+cudaError_t jsh_launch_plane(const JshRequest* d_reqs, int n_req, uint64_t max_along, cudaStream_t stream) {
+  if (n_req <= 0) return cudaSuccess;
+  plane_along_kernel<<<n_req, 32, 0, stream>>>(d_reqs);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  dim3 g((unsigned)((max_along + kPlaneThreads - 1) / kPlaneThreads), (unsigned)n_req);
+  plane_across_kernel<<<g, kPlaneThreads, 0, stream>>>(d_reqs);
+  return cudaGetLastError();
+}
+
+cudaError_t jsh_launch_hit(const JshRequest* d_reqs, int n_req, uint64_t max_pix, cudaStream_t stream) {
+  if (n_req <= 0 || max_pix == 0) return cudaSuccess;
+  dim3 g((unsigned)((max_pix + kHitThreads - 1) / kHitThreads), (unsigned)n_req);
+  hit_kernel<<<g, kHitThreads, 0, stream>>>(d_reqs);
+  return cudaGetLastError();
+}
+
+cudaError_t jsh_launch_transfer(const JshRequest* d_reqs, int n_req, int precision, int schedule, bool full,
+                                uint64_t max_items, const JshLaunchShape& shape, unsigned int* queue,
+                                int num_sms, cudaStream_t stream) {
+  if (n_req <= 0 || max_items == 0) return cudaSuccess;
+  if (precision == JSH_PREC_MIXED)
+    return jsh_launch_transfer_mixed(d_reqs, n_req, schedule, full, max_items, shape, queue, num_sms, stream);
+  if (schedule == JSH_SCHED_PERSISTENT)
+    return jsh_launch_transfer_persistent64(d_reqs, n_req, max_items, shape, queue, num_sms, stream);
+  const int bs = 128;
+  uint64_t blocks = (max_items + bs - 1) / bs;
+  transfer_static64_kernel<<<(unsigned)blocks, bs, 0, stream>>>(d_reqs, n_req);
+  return cudaGetLastError();
+}
+
+cudaError_t jsh_launch_hit_rays(const JshModel& model, const double* d_orig, const double* d_dir, int64_t n,
+                                int32_t* d_nseg, double* d_seg, uint32_t* d_status, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  hit_rays_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(model, d_orig, d_dir, n, d_nseg, d_seg,
+                                                                    d_status);
+  return cudaGetLastError();
+}
+
+cudaError_t jsh_launch_plane_rays(const JshPlane& plane, double* d_orig, double* d_sizes, cudaStream_t stream) {
+  uint64_t npix = plane.n_across * plane.n_along;
+  if (npix == 0) return cudaSuccess;
+  plane_rays_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, stream>>>(plane, d_orig, d_sizes);
+  return cudaGetLastError();
+}
+
+cudaError_t jsh_launch_grid_interp(const JshGrid& grid, int field, const double* d_zr, int64_t n, double nan_value,
+                                   double* d_out, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  grid_interp_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(grid, field, d_zr, n, nan_value, d_out);
+  return cudaGetLastError();
+}

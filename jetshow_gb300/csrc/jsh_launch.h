@@ -1,0 +1,49 @@
+// jsh_launch.h -- host-callable launchers of the device kernels.  A batch is
+// an array of JshRequest in device memory; every launcher enqueues on
+// `stream` and returns the cudaError_t of the launch.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "jsh_request.h"
+
+#define JSH_MAX_BATCH 64
+
+struct JshLaunchShape {
+  int block_size;        // threads per CTA of the transfer kernel
+  int ctas_per_sm;       // persistent schedule: CTAs per SM (0: occupancy max)
+  int refill_threshold;  // persistent schedule: refill when >= this many lanes idle
+};
+
+// Ray generation: along sizes and centres (sequential recurrence of
+// pyLogspace / partial_sum), then the across-centre table.  max_along is
+// the largest n_along of the batch.
+cudaError_t jsh_launch_plane(const JshRequest* d_reqs, int n_req, uint64_t max_along, cudaStream_t stream);
+
+// Hit every pixel's ray against the request's geometry, append the hit rays
+// to req.hits (count in *req.n_hit, zeroed beforehand), write the outputs of
+// missing pixels (zeros and geometry status) for every frequency.
+cudaError_t jsh_launch_hit(const JshRequest* d_reqs, int n_req, uint64_t max_pix, cudaStream_t stream);
+
+// Transfer every (hit ray, frequency) of the batch.  `queue` is a zeroed
+// device counter used by the persistent schedule; max_items bounds the
+// total work items (sum of npix * n_nu) for the static grid.
+cudaError_t jsh_launch_transfer(const JshRequest* d_reqs, int n_req, int precision, int schedule, bool full,
+                                uint64_t max_items, const JshLaunchShape& shape, unsigned int* queue,
+                                int num_sms, cudaStream_t stream);
+
+// Hit arbitrary rays (origins/directions device arrays, directions already
+// normalised on the device by this kernel as Ray::Ray does).
+cudaError_t jsh_launch_hit_rays(const JshModel& model, const double* d_orig, const double* d_dir, int64_t n,
+                                int32_t* d_nseg, double* d_seg, uint32_t* d_status, cudaStream_t stream);
+
+// Plane rays (origins, sizes) of one compiled plane whose along/across tables
+// are filled.
+cudaError_t jsh_launch_plane_rays(const JshPlane& plane, double* d_orig, double* d_sizes, cudaStream_t stream);
+
+// Gridded field interpolation at (z, r) points.
+cudaError_t jsh_launch_grid_interp(const JshGrid& grid, int field, const double* d_zr, int64_t n,
+                                   double nan_value, double* d_out, cudaStream_t stream);
+
+// Largest resident CTAs per SM of the persistent transfer kernel.
+int jsh_persistent_occupancy(int precision, bool full, int block_size);

@@ -1,0 +1,126 @@
+"""Process-level handle on the C-ABI context (``jsh_ctx``) and the calls the
+Python host side makes through it.  Results come back as numpy arrays
+shaped [n_nu, n_across, n_along]."""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+
+from . import _capi as A
+
+PLANES = ("tau", "l", "I", "Q", "U", "V")
+
+
+class JetshowError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"jetshow_gb300 error {status}: {msg}")
+        self.status = status
+
+
+def check(lib, st):
+    if st != 0:
+        raise JetshowError(st, (lib.jsh_last_error() or b"").decode(errors="replace"))
+    return st
+
+
+class Context:
+    """Owns one ``jsh_ctx`` on a CUDA device."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = A.load_library()
+        h = C.c_void_p()
+        check(self.lib, self.lib.jsh_ctx_create(device, hbm_budget_bytes, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self.lib.jsh_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------- render
+    def render(self, model: A.ModelDesc, plane: A.PlaneDesc, nu, params: A.Params, want=PLANES):
+        nu = np.ascontiguousarray(np.atleast_1d(nu), dtype=np.float64)
+        na, nl = int(plane.n_across), int(plane.n_along)
+        out = {k: np.zeros((nu.size, na, nl)) for k in want}
+        out["status"] = np.zeros((nu.size, na, nl), np.uint32)
+        img = A.Image(*(A.dptr(out[k]) if k in out else None for k in PLANES),
+                      out["status"].ctypes.data_as(C.POINTER(C.c_uint32)))
+        st = A.Stats()
+        check(self.lib, self.lib.jsh_observation_run(self.handle, C.byref(model), C.byref(plane),
+                                                     A.dptr(nu), nu.size, C.byref(params), C.byref(img),
+                                                     C.byref(st)))
+        return out, stats_dict(st)
+
+    def render_device(self, model, plane, nu, params, stream_ptr, dev_planes: dict):
+        """Enqueue a render on a CUDA stream with device output pointers
+        (``dev_planes`` maps plane names to raw device addresses)."""
+        nu = np.ascontiguousarray(np.atleast_1d(nu), dtype=np.float64)
+        img = A.DeviceImage(*(dev_planes.get(k) for k in PLANES), dev_planes.get("status"))
+        check(self.lib, self.lib.jsh_observation_run_device(self.handle, C.byref(model), C.byref(plane),
+                                                            A.dptr(nu), nu.size, C.byref(params),
+                                                            C.c_void_p(stream_ptr), C.byref(img)))
+
+    def last_stats(self):
+        st = A.Stats()
+        check(self.lib, self.lib.jsh_last_stats(self.handle, C.byref(st)))
+        return stats_dict(st)
+
+    # ----------------------------------------------------- inspection
+    def plane_rays(self, plane: A.PlaneDesc):
+        n = int(plane.n_across * plane.n_along)
+        o = np.zeros((n, 3)); d = np.zeros(3); s = np.zeros(n)
+        check(self.lib, self.lib.jsh_plane_rays(self.handle, C.byref(plane), A.dptr(o), A.dptr(d), A.dptr(s)))
+        return o, d, s
+
+    def trace_plane(self, model: A.ModelDesc, plane: A.PlaneDesc):
+        n = int(plane.n_across * plane.n_along)
+        nseg = np.zeros(n, np.int32); seg = np.zeros((n, 2, 2, 3)); st = np.zeros(n, np.uint32)
+        check(self.lib, self.lib.jsh_trace_plane(self.handle, C.byref(model), C.byref(plane),
+                                                 nseg.ctypes.data_as(C.POINTER(C.c_int32)), A.dptr(seg),
+                                                 st.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return nseg, seg, st
+
+    def hit_rays(self, model: A.ModelDesc, origins, directions):
+        origins = np.ascontiguousarray(origins, dtype=np.float64)
+        directions = np.ascontiguousarray(directions, dtype=np.float64)
+        n = origins.shape[0]
+        nseg = np.zeros(n, np.int32); seg = np.zeros((n, 2, 2, 3)); st = np.zeros(n, np.uint32)
+        check(self.lib, self.lib.jsh_hit_rays(self.handle, C.byref(model), A.dptr(origins), A.dptr(directions),
+                                              n, nseg.ctypes.data_as(C.POINTER(C.c_int32)), A.dptr(seg),
+                                              st.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return nseg, seg, st
+
+
+def stats_dict(st: A.Stats) -> dict:
+    return {f: getattr(st, f) for f, _ in A.Stats._fields_}
+
+
+_default = None
+_lock = threading.Lock()
+
+
+def default_context() -> Context:
+    global _default
+    with _lock:
+        if _default is None:
+            _default = Context(0)
+        return _default
+
+
+def mas_to_pc(z: float, H0=None, omega_M=None, omega_V=None, gamma_nu=None) -> float:
+    """Parsecs per mas at redshift z (jsh_mas_to_pc; reference defaults when
+    no cosmology is given)."""
+    lib = A.load_library()
+    if H0 is None:
+        return lib.jsh_mas_to_pc(z, None)
+    cosmo = A.Cosmology(H0=H0, omega_M=omega_M, omega_V=omega_V, gamma_nu=gamma_nu or 0.0)
+    return lib.jsh_mas_to_pc(z, C.byref(cosmo))

@@ -1,0 +1,85 @@
+/*
+ * jsh_oracle.h -- TEST INFRASTRUCTURE.  A plain-C, all-FP64 CPU restatement
+ * of jetshow's per-pixel transfer path, used only as the checker of the GPU
+ * library (tests, the smoke check and the CPU-baseline leg of bench.py).
+ * Nothing in the product links or calls it.
+ *
+ * Parity status: the reference itself cannot be compiled here (it needs
+ * Boost.odeint, Eigen and CGAL, none of which is installed), so this
+ * restatement is pinned by (a) the reference's own golden vectors, the
+ * Cone::hit cases of tests/simple_test.cpp:17-101, and (b) analytic known
+ * answers of the transfer equations (see tests/test_oracle.py).  Transfer
+ * parity beyond those is otherwise unpinned.
+ *
+ * The descriptor structs are the C-ABI's (include/jetshow_capi.h); the code
+ * is independent of the product's.
+ */
+#ifndef JSH_ORACLE_H
+#define JSH_ORACLE_H
+
+#include "../include/jetshow_capi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct jo_counters {
+  uint64_t rhs_evals;
+  uint64_t steps_accepted;
+  uint64_t steps_rejected;
+} jo_counters;
+
+/* Image plane rays (ImagePlane/Image/Ray constructors).  origins[npix][3],
+ * direction[3], sizes[npix]; any pointer may be NULL. */
+int jo_plane_rays(const jsh_plane_desc* plane, double* origins, double* direction,
+                  double* sizes);
+
+/* Hit of arbitrary rays; directions are normalised as Ray::Ray does. */
+int jo_hit_rays(const jsh_model_desc* model, const double* origins,
+                const double* directions, int64_t n, int32_t* n_seg, double* seg,
+                uint32_t* status);
+
+/* Render the pixels pix_idx[0..n_sel) (NULL: all pixels, n_sel ignored) of
+ * the plane at n_nu frequencies.  Output planes are [n_nu][n_sel].
+ * n_threads <= 0: OpenMP default.  Returns 0 or a negative status. */
+int jo_render(const jsh_model_desc* model, const jsh_plane_desc* plane,
+              const double* nu, int32_t n_nu, const jsh_params* params,
+              const int64_t* pix_idx, int64_t n_sel, int32_t n_threads,
+              jsh_image* out, jo_counters* counters);
+
+/* All eleven transfer coefficients at a lab-frame point for the LOS unit
+ * vector n_los (pointing to the observer) and frequency nu:
+ * out = {kI, kQ, kU, kV, kF, kC, hQ, etaI, etaQ, etaU, etaV}. */
+int jo_coefficients(const jsh_model_desc* model, const double* point,
+                    const double* n_los, double nu, double* out);
+
+/* Integrate dx/dt = a x + b (scalar) from 0 to L with the tau-pass machinery
+ * (dense-output Dormand-Prince, odeint adaptive-range semantics) and return
+ * x(L); used by the known-answer tests of the integrator. */
+double jo_test_linear_dense(double a, double b, double L, double dt0,
+                            double atol, double rtol, int64_t* n_steps);
+/* Same with the controlled stepper of integrate_adaptive. */
+double jo_test_linear_controlled(double a, double b, double L, double dt0,
+                                 double atol, double rtol, int64_t* n_steps);
+/* One Dormand-Prince step of x' = x from x=1 over h, then the dense output
+ * at theta: returns dense(theta) - exp(theta*h). */
+double jo_test_dense_error(double h, double theta);
+
+/* Parsecs per mas at redshift z (NULL cosmo: the reference defaults). */
+double jo_mas_to_pc(double z, const jsh_cosmology* cosmo);
+
+/* Register a triangulated (z, r) grid under `grid_id` (0..15) for the
+ * JSH_*_SIMULATION fields.  xy[n][2] in pc, values[n][n_fields]. */
+int jo_grid_register(int32_t grid_id, const double* xy, int64_t n,
+                     const float* values, int32_t n_fields, const int32_t* tri,
+                     int64_t n_tri);
+double jo_grid_value(int32_t grid_id, int32_t field, double z_pc, double r_pc,
+                     double nan_value);
+
+int jo_openmp_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

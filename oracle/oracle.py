@@ -1,0 +1,146 @@
+"""TEST INFRASTRUCTURE: ctypes loader of the CPU oracle (``oracle/jsh_oracle.c``).
+
+Only the test suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module, and only as the checker.  The oracle is an
+FP64 restatement of the reference path; parity is pinned by the reference's
+Cone::hit golden vectors and by analytic known answers (see ``tests/``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from jetshow_gb300 import _capi as A
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libjsh_oracle.so")
+
+
+class Counters(C.Structure):
+    _fields_ = [("rhs_evals", C.c_uint64), ("steps_accepted", C.c_uint64),
+                ("steps_rejected", C.c_uint64)]
+
+
+def build(quiet: bool = True) -> str:
+    """Compile the oracle with its Makefile (gcc, -ffp-contract=off, OpenMP)."""
+    r = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        # retry without OpenMP (a toolchain without libgomp)
+        r = subprocess.run(["make", "-C", HERE, "OMPFLAGS="], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        P, D = C.POINTER, C.POINTER(C.c_double)
+        L.jo_plane_rays.argtypes = [P(A.PlaneDesc), D, D, D]
+        L.jo_hit_rays.argtypes = [P(A.ModelDesc), D, D, C.c_int64, P(C.c_int32), D, P(C.c_uint32)]
+        L.jo_render.argtypes = [P(A.ModelDesc), P(A.PlaneDesc), D, C.c_int32, P(A.Params),
+                                P(C.c_int64), C.c_int64, C.c_int32, P(A.Image), P(Counters)]
+        L.jo_coefficients.argtypes = [P(A.ModelDesc), D, D, C.c_double, D]
+        L.jo_test_linear_dense.argtypes = [C.c_double] * 6 + [P(C.c_int64)]
+        L.jo_test_linear_dense.restype = C.c_double
+        L.jo_test_linear_controlled.argtypes = [C.c_double] * 6 + [P(C.c_int64)]
+        L.jo_test_linear_controlled.restype = C.c_double
+        L.jo_test_dense_error.argtypes = [C.c_double, C.c_double]
+        L.jo_test_dense_error.restype = C.c_double
+        L.jo_mas_to_pc.argtypes = [C.c_double, P(A.Cosmology)]
+        L.jo_mas_to_pc.restype = C.c_double
+        L.jo_grid_register.argtypes = [C.c_int32, D, C.c_int64, P(C.c_float), C.c_int32,
+                                       P(C.c_int32), C.c_int64]
+        L.jo_grid_value.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double]
+        L.jo_grid_value.restype = C.c_double
+        L.jo_openmp_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _chk(st):
+    if st != 0:
+        raise RuntimeError(f"oracle call failed with status {st}")
+
+
+def plane_rays(plane: A.PlaneDesc):
+    n = int(plane.n_across * plane.n_along)
+    o = np.zeros((n, 3)); d = np.zeros(3); s = np.zeros(n)
+    _chk(lib().jo_plane_rays(C.byref(plane), A.dptr(o), A.dptr(d), A.dptr(s)))
+    return o, d, s
+
+
+def hit_rays(model: A.ModelDesc, origins, directions):
+    origins = np.ascontiguousarray(origins, dtype=np.float64)
+    directions = np.ascontiguousarray(directions, dtype=np.float64)
+    n = origins.shape[0]
+    nseg = np.zeros(n, np.int32); seg = np.zeros((n, 2, 2, 3)); st = np.zeros(n, np.uint32)
+    _chk(lib().jo_hit_rays(C.byref(model), A.dptr(origins), A.dptr(directions), n,
+                           nseg.ctypes.data_as(C.POINTER(C.c_int32)), A.dptr(seg),
+                           st.ctypes.data_as(C.POINTER(C.c_uint32))))
+    return nseg, seg, st
+
+
+def render(model: A.ModelDesc, plane: A.PlaneDesc, nu, params: A.Params, pix=None, threads=0):
+    """Render (all pixels or the flat pixel indices ``pix``); returns a dict of
+    [n_nu, n_sel] arrays plus counters."""
+    nu = np.ascontiguousarray(np.atleast_1d(nu), dtype=np.float64)
+    npix = int(plane.n_across * plane.n_along)
+    if pix is None:
+        nsel = npix
+        pix_p = None
+    else:
+        pix = np.ascontiguousarray(pix, dtype=np.int64)
+        nsel = pix.size
+        pix_p = pix.ctypes.data_as(C.POINTER(C.c_int64))
+    out = {k: np.zeros((nu.size, nsel)) for k in ("tau", "l", "I", "Q", "U", "V")}
+    out["status"] = np.zeros((nu.size, nsel), np.uint32)
+    img = A.Image(*(A.dptr(out[k]) for k in ("tau", "l", "I", "Q", "U", "V")),
+                  out["status"].ctypes.data_as(C.POINTER(C.c_uint32)))
+    cnt = Counters()
+    _chk(lib().jo_render(C.byref(model), C.byref(plane), A.dptr(nu), nu.size, C.byref(params),
+                         pix_p, nsel, threads, C.byref(img), C.byref(cnt)))
+    out["rhs_evals"] = cnt.rhs_evals
+    out["steps_accepted"] = cnt.steps_accepted
+    out["steps_rejected"] = cnt.steps_rejected
+    return out
+
+
+def coefficients(model, point, n_los, nu):
+    out = np.zeros(11)
+    p = np.ascontiguousarray(point, dtype=np.float64)
+    n = np.ascontiguousarray(n_los, dtype=np.float64)
+    _chk(lib().jo_coefficients(C.byref(model), A.dptr(p), A.dptr(n), nu, A.dptr(out)))
+    return out
+
+
+def mas_to_pc(z, cosmo=None):
+    return lib().jo_mas_to_pc(z, C.byref(cosmo) if cosmo is not None else None)
+
+
+def grid_register(grid_id, xy, values, tri):
+    xy = np.ascontiguousarray(xy, dtype=np.float64)
+    values = np.ascontiguousarray(values, dtype=np.float32)
+    if values.ndim == 1:
+        values = values[:, None]
+    tri = np.ascontiguousarray(tri, dtype=np.int32)
+    _chk(lib().jo_grid_register(grid_id, A.dptr(xy), xy.shape[0],
+                                values.ctypes.data_as(C.POINTER(C.c_float)), values.shape[1],
+                                tri.ctypes.data_as(C.POINTER(C.c_int32)), tri.shape[0]))
+
+
+def grid_value(grid_id, field, z_pc, r_pc, nan_value=0.0):
+    return lib().jo_grid_value(grid_id, field, z_pc, r_pc, nan_value)
+
+
+def threads():
+    return lib().jo_openmp_threads()
