@@ -69,6 +69,8 @@ void jsh_request_layout(uint64_t npix, uint64_t n_along, uint64_t n_across, int3
   o = align_up(o + sizeof(uint32_t));
   L->off_nu = o;
   o = align_up(o + sizeof(double) * n_nu);
+  L->off_fc = o;
+  o = align_up(o + sizeof(JshFreqConst) * n_nu);
   L->off_along_size = o;
   o = align_up(o + sizeof(double) * n_along);
   L->off_along_center = o;
@@ -89,6 +91,7 @@ void jsh_bind_request(JshRequest* req, char* base, const JshRequestLayout& L, bo
   req->counters = (unsigned long long*)(base + L.off_counters);
   req->n_hit = (uint32_t*)(base + L.off_nhit);
   req->nu = (const double*)(base + L.off_nu);
+  req->mix.fc = (const JshFreqConst*)(base + L.off_fc);
   req->plane.along_size = (double*)(base + L.off_along_size);
   req->plane.along_center = (double*)(base + L.off_along_center);
   req->plane.across_pos = (double*)(base + L.off_across);
@@ -192,10 +195,6 @@ int jsh_prepare_request(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_pla
   return JSH_OK;
 }
 
-// Prepare per-frequency constants of the mixed-precision path (declared in
-// jsh_persistent.cu); fills req->mixed from the compiled model and nu.
-int jsh_prepare_mixed(JshRequest* req, const double* nu_host);
-
 extern "C" int jsh_ctx_create(int device, uint64_t hbm_budget_bytes, jsh_ctx** out) {
   if (!out) {
     jsh_set_error("null output pointer");
@@ -230,6 +229,7 @@ extern "C" int jsh_ctx_create(int device, uint64_t hbm_budget_bytes, jsh_ctx** o
       cudaEventCreate(&c->ev_start) != cudaSuccess || cudaEventCreate(&c->ev_stop) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ws_ready, cudaEventDisableTiming) != cudaSuccess ||
       cudaMallocHost((void**)&c->h_req, sizeof(JshRequest)) != cudaSuccess ||
+      cudaMallocHost((void**)&c->h_fc, 4096 * sizeof(JshFreqConst)) != cudaSuccess ||
       cudaMallocHost((void**)&c->h_counters, 8 * sizeof(unsigned long long)) != cudaSuccess) {
     jsh_set_error("context creation failed: %s", cudaGetErrorString(cudaGetLastError()));
     jsh_ctx_destroy(c);
@@ -249,6 +249,7 @@ extern "C" void jsh_ctx_destroy(jsh_ctx* c) {
   for (auto& g : c->grids)
     if (g.used) jsh_free_device(c, g.mem, g.bytes);
   if (c->h_req) cudaFreeHost(c->h_req);
+  if (c->h_fc) cudaFreeHost(c->h_fc);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->ev_start) cudaEventDestroy(c->ev_start);
   if (c->ev_stop) cudaEventDestroy(c->ev_stop);
@@ -303,14 +304,16 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
     req.V = dev_out->V;
     req.status = dev_out->status;
   }
-  if (params->precision == JSH_PREC_MIXED) {
-    st = jsh_prepare_mixed(&req, nu_hz);
-    if (st) return st;
-  }
   // the previous user of the workspace (possibly on another stream) must finish
   JSH_CUDA_TRY(cudaStreamWaitEvent(stream, ctx->ws_ready, 0));
-  // the pinned staging buffer is reused: wait for its previous copy
+  // the pinned staging buffers are reused: wait for their previous copies
   JSH_CUDA_TRY(cudaEventSynchronize(ctx->ws_ready));
+  if (params->precision == JSH_PREC_MIXED) {
+    st = jsh_prepare_mixed(&req, nu_hz, ctx->h_fc);
+    if (st) return st;
+    JSH_CUDA_TRY(cudaMemcpyAsync(base + L.off_fc, ctx->h_fc, sizeof(JshFreqConst) * n_nu, cudaMemcpyHostToDevice,
+                                 stream));
+  }
   *ctx->h_req = req;
   JSH_CUDA_TRY(cudaMemcpyAsync(base + L.off_req, ctx->h_req, sizeof(JshRequest), cudaMemcpyHostToDevice, stream));
   JSH_CUDA_TRY(cudaMemcpyAsync(base + L.off_nu, nu_hz, sizeof(double) * n_nu, cudaMemcpyHostToDevice, stream));

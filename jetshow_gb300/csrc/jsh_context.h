@@ -28,7 +28,7 @@ struct JshGridSlot {
 
 // Layout of one request's device memory inside an arena allocation.
 struct JshRequestLayout {
-  size_t off_req, off_counters, off_nhit, off_queue, off_nu, off_along_size, off_along_center, off_across,
+  size_t off_req, off_counters, off_nhit, off_queue, off_nu, off_fc, off_along_size, off_along_center, off_across,
       off_hits, off_out[7];
   size_t total;
   bool own_outputs;
@@ -45,6 +45,7 @@ struct jsh_ctx {
   void* ws = nullptr;  // workspace of the blocking / device entry points
   size_t ws_cap = 0;
   JshRequest* h_req = nullptr;               // pinned staging of one request
+  JshFreqConst* h_fc = nullptr;              // pinned staging of its frequency constants [4096]
   unsigned long long* h_counters = nullptr;  // pinned [8]
   JshGridSlot grids[JSH_MAX_GRIDS];
   bool tuned = false;
@@ -63,6 +64,9 @@ void jsh_request_layout(uint64_t npix, uint64_t n_along, uint64_t n_across, int3
                         JshRequestLayout* L);
 void jsh_bind_request(JshRequest* req, char* base, const JshRequestLayout& L, bool own_outputs);
 int jsh_alloc_device(jsh_ctx* ctx, size_t bytes, void** p);
+// Mixed-precision constants of a prepared request: fills req->mix (except
+// the device pointer fc) and fc_host[n_nu].
+int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc_host);
 void jsh_free_device(jsh_ctx* ctx, void* p, size_t bytes);
 JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params);
 void jsh_set_error(const char* fmt, ...);

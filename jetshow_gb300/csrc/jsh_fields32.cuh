@@ -1,0 +1,300 @@
+// jsh_fields32.cuh -- FP32 field laws and transfer coefficients of the
+// mixed-precision path.  Lengths are in pc, intensities in units of the
+// per-frequency scale S (JshFreqConst::scale).
+//
+// Coefficient algebra.  With b = |n'_los x B'| (B', n' in the plasma frame),
+// w = b D, P = w^((s+2)/2) and R = w^((s+1)/2) = P / sqrt(w), the lab-frame
+// coefficients of src/utils.cpp:39-143 with k = k'/D and eta = eta' D^2
+// (src/Jet.cpp:15-46, :218-237) collapse to
+//   k_I   = a_k  n' P                      eta_I = a_e n' R D
+//   k_Q   = q_k k_I                        eta_Q = q_e eta_I
+//   k_V   = -a_v n' B_par R D              eta_V = -a_ev n' B_par D^2 P / w
+//   k_F   =  a_f n' B_par D                k_C   = -a_c n' (c1 w^2 - c2 P)
+// (B_par = B'.n'_los), where the a_* hold every frequency-dependent power,
+// the tgamma factors, the cgs constants and the unit scales; they are
+// computed once per frequency on the host in FP64.  One log2, one exp2 and
+// one rsqrt per evaluation replace the reference's pow and tgamma calls.
+// Velocities are carried as (Gamma, unit direction) so that
+// 1 - beta.n = (1 - beta) + beta |v_hat - n|^2 / 2 with
+// 1 - beta = 1 / (Gamma^2 (1 + beta)) stays accurate in FP32.
+#pragma once
+
+#include "jsh_request.h"
+
+namespace jsh {
+
+struct F3 {
+  float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float fdot(F3 a, F3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ F3 fcross(F3 a, F3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+// x^e for x > 0 by exp2(e log2 x); NaN for x < 0 like pow with a
+// non-integer exponent, 0 -> +inf / 0 as pow.
+__device__ __forceinline__ float fpow(float x, float e) { return exp2f(e * __log2f(x)); }
+
+// (z, r) in pc on the FP64 bucket grid
+__device__ inline float sim32(const JshGrid& G, int field, F3 p, float nan_value) {
+  double r = sqrt((double)p.x * p.x + (double)p.y * p.y);
+  return (float)grid_value(G, field, (double)p.z, r, nan_value);
+}
+
+// ---------------------------------------------------------------- V
+struct Vel {
+  float gamma;
+  F3 dir;  // unit
+};
+
+__device__ __forceinline__ F3 parabolic_dir(float Rz0_pc, F3 p) {
+  float r = hypotf(p.x, p.y);
+  if (r == 0.f) return f3(0.f, 0.f, 1.f);
+  float R = sqrtf(Rz0_pc * Rz0_pc * p.z);
+  float r0 = Rz0_pc * r / R;
+  float alpha = atanf(2.f * r / r0 / r0);
+  float sa, ca;
+  sincosf(alpha, &sa, &ca);
+  return f3(ca * p.x / r, ca * p.y / r, sa);
+}
+
+__device__ inline Vel vfield32(const JshModel& m, F3 p) {
+  const double* q = m.vp;
+  const float inv_pc = (float)(1.0 / JSH_PC);
+  switch (m.v_kind) {
+    case JSH_V_CONST_FLAT: return Vel{(float)q[0], f3(0, 0, 1)};
+    case JSH_V_SHEARED_FLAT: {
+      float r = sqrtf(p.x * p.x + p.y * p.y);
+      float g = (float)q[0] - (float)(q[0] - q[1]) * r / (float)(q[2] / JSH_PC);
+      return Vel{g, f3(0, 0, 1)};
+    }
+    case JSH_V_SHEATH_FLAT: {
+      float r = sqrtf(p.x * p.x + p.y * p.y);
+      return Vel{r < (float)(q[2] / JSH_PC) ? (float)q[0] : (float)q[1], f3(0, 0, 1)};
+    }
+    case JSH_V_CONST_CENTRAL: {
+      F3 a = p + f3((float)q[1], (float)q[2], (float)q[3]) * inv_pc;
+      return Vel{(float)q[0], a * rsqrtf(fdot(a, a))};
+    }
+    case JSH_V_SHEARED_CENTRAL: {
+      // theta = acos(z + o_z / r) evaluated in cm as written (src/VField.cpp:83)
+      F3 a = p + f3((float)q[3], (float)q[4], (float)q[5]) * inv_pc;
+      float r_cm = sqrtf(fdot(a, a)) * (float)JSH_PC;
+      float theta = acosf(p.z * (float)JSH_PC + (float)q[5] / r_cm);
+      float g = (float)q[0] - (float)(q[0] - q[1]) * theta / (float)q[2];
+      return Vel{g, a * rsqrtf(fdot(a, a))};
+    }
+    case JSH_V_SHEATH_CENTRAL: {
+      F3 a = p + f3((float)q[3], (float)q[4], (float)q[5]) * inv_pc;
+      float r = sqrtf(fdot(a, a));
+      float theta = acosf(p.z / r);
+      return Vel{theta < (float)q[2] ? (float)q[0] : (float)q[1], a * (1.f / r)};
+    }
+    case JSH_V_CONST_PARABOLIC: return Vel{(float)q[0], parabolic_dir((float)(q[1] / JSH_PC), p)};
+    case JSH_V_ACC_PARABOLIC: {
+      float g = 1.f + (float)(q[0] - 1.0) * sqrtf(p.z / (float)(q[1] / JSH_PC));
+      return Vel{g, parabolic_dir((float)(q[2] / JSH_PC), p)};
+    }
+    case JSH_V_SHEARED_ACC_PARABOLIC:
+    case JSH_V_SHEARED_ACC_PARABOLIC_CONST_CONE:
+    case JSH_V_ACC_PARABOLIC_CONST_CONE: {
+      int k = m.v_kind;
+      float z0_pc = (float)((k == JSH_V_ACC_PARABOLIC_CONST_CONE ? q[2] : q[3]) / JSH_PC);
+      if (k != JSH_V_SHEARED_ACC_PARABOLIC && p.z > z0_pc) {
+        F3 a = p + f3(0.f, 0.f, (float)(m.v_cone_oz / JSH_PC));
+        F3 dir = a * rsqrtf(fdot(a, a));
+        if (k == JSH_V_ACC_PARABOLIC_CONST_CONE) return Vel{(float)q[0], dir};
+        float r_cm = sqrtf(fdot(a, a)) * (float)JSH_PC;
+        float theta = acosf(p.z * (float)JSH_PC + (float)m.v_cone_oz / r_cm);
+        return Vel{(float)q[0] - (float)(q[0] - q[1]) * theta / (float)m.v_theta, dir};
+      }
+      if (k == JSH_V_ACC_PARABOLIC_CONST_CONE) {
+        float g = 1.f + (float)(q[0] - 1.0) * sqrtf(p.z / z0_pc);
+        return Vel{g, parabolic_dir((float)(q[1] / JSH_PC), p)};
+      }
+      float R0_pc = (k == JSH_V_SHEARED_ACC_PARABOLIC) ? (float)(q[2] / JSH_PC) : z0_pc;
+      float Rz0_pc = (float)((k == JSH_V_SHEARED_ACC_PARABOLIC ? q[3] : q[2]) / JSH_PC);
+      float r = hypotf(p.x, p.y);
+      float R = sqrtf(Rz0_pc * Rz0_pc * p.z);
+      float g0 = (float)q[0] - (float)(q[0] - q[1]) * sqrtf(sqrtf(r / R));
+      if (g0 < 1.f) g0 = 1.f;
+      float g = 1.f + (g0 - 1.f) * sqrtf(p.z / R0_pc);
+      return Vel{g, parabolic_dir(Rz0_pc, p)};
+    }
+    case JSH_V_SIMULATION: return Vel{sim32(m.grids[2], m.f_v, p, 1.0f), f3(0, 0, 1)};
+    default: return Vel{1.f, f3(0, 0, 1)};
+  }
+}
+
+// ---------------------------------------------------------------- N
+__device__ inline float nfield32(const JshModel& m, F3 p) {
+  const double* q = m.np;
+  switch (m.n_kind) {
+    case JSH_N_CONST: return (float)q[0];
+    case JSH_N_BK: return (float)q[0] * fpow(sqrtf(fdot(p, p)), -(float)q[1]);
+    case JSH_N_BKZ: return (float)q[0] * fpow(fabsf(p.z), -(float)q[1]);
+    case JSH_N_COMPOSITE_BK: {
+      float e = (fabsf(p.z) > (float)(q[3] / JSH_PC)) ? (float)q[2] : (float)q[1];
+      return (float)q[0] * fpow(sqrtf(fdot(p, p)), -e);
+    }
+    case JSH_N_SIMULATION: return sim32(m.grids[1], m.f_n, p, 0.0f);
+    default: return 0.f;
+  }
+}
+
+// ---------------------------------------------------------------- B
+__device__ inline float bscalar32(const JshModel& m, F3 p) {
+  const double* q = m.bp;
+  switch (m.b_kind) {
+    case JSH_B_RANDOM_SCALAR: return (float)q[0] * fpow(sqrtf(fdot(p, p)), -(float)q[1]);
+    case JSH_B_RANDOM_SCALAR_Z: return (float)q[0] * fpow(fabsf(p.z), -(float)q[1]);
+    case JSH_B_COMPOSITE_RANDOM_SCALAR_Z: {
+      float e = (fabsf(p.z) > (float)(q[3] / JSH_PC)) ? (float)q[2] : (float)q[1];
+      return (float)q[0] * fpow(fabsf(p.z), -e);
+    }
+    default: return 0.f;
+  }
+}
+
+// sin and cos of atan(u): u / sqrt(1 + u^2), 1 / sqrt(1 + u^2)
+__device__ __forceinline__ void sincos_atan(float u, float& s, float& c) {
+  if (isinf(u)) {
+    s = u > 0 ? 1.f : -1.f;
+    c = 0.f;
+    return;
+  }
+  c = rsqrtf(fmaf(u, u, 1.f));
+  s = u * c;
+}
+
+__device__ inline F3 bvector32(const JshModel& m, F3 p) {
+  const double* q = m.bp;
+  switch (m.b_kind) {
+    case JSH_B_CONST_CYLINDER: return f3(0, 0, (float)q[0] * fpow(sqrtf(fdot(p, p)), -(float)q[1]));
+    case JSH_B_CONST_CYLINDER_Z: return f3(0, 0, (float)q[0] * fpow(fabsf(p.z), -(float)q[1]));
+    case JSH_B_RADIAL_CONICAL: {
+      float r = sqrtf(fdot(p, p));
+      return p * ((float)q[0] * fpow(r, -(float)q[1]) / r);
+    }
+    case JSH_B_TOROIDAL: {
+      float s, c;
+      sincos_atan(p.y / p.x, s, c);
+      float b = (float)q[0] * fpow(p.z, -(float)q[1]);
+      return f3(-s * b, c * b, 0.f);
+    }
+    case JSH_B_HELICAL_CYLINDER: {
+      float r = sqrtf(p.x * p.x + p.y * p.y);
+      float b0 = (float)q[0], pa = (float)q[1];
+      return f3(b0 * tanf(pa * p.y / r), -b0 * tanf(pa * p.x / r), b0);
+    }
+    case JSH_B_SPIRAL_CONICAL: {
+      float bz = (float)q[0] / (p.z * p.z);
+      float tp = (float)m.tan_pitch;
+      return f3(bz * (p.x / p.z + p.y * tp), bz * (p.y / p.z - p.x * tp), bz);
+    }
+    case JSH_B_FORCE_FREE_CYLINDRICAL: {
+      float s, c;
+      sincos_atan(p.y / p.x, s, c);
+      float b1 = (float)(q[0] * m.bessel1);
+      return f3(-b1 * s, b1 * s, (float)(q[0] * m.bessel0));
+    }
+    case JSH_B_HELICAL_CONICAL: {
+      float b = (float)q[0] * fpow(sqrtf(fdot(p, p)), -(float)q[1]);
+      float rc2 = p.x * p.x + p.y * p.y;
+      float px = 0.f, py = 0.f;
+      if (rc2 > 0.f) {
+        float irc = rsqrtf(rc2);
+        px = -p.y * irc;
+        py = p.x * irc;
+        if (q[3] != 0.0 && p.x < 0.f) {
+          px = -px;
+          py = -py;
+        }
+      }
+      float bt = b * (float)m.sin_pitch;
+      return f3(bt * px, bt * py, b * (float)m.cos_pitch);
+    }
+    case JSH_B_SIMULATION: {
+      float s, c;
+      sincos_atan(p.y / p.x, s, c);
+      float bp = sim32(m.grids[0], m.fb_p, p, 0.f);
+      float bphi = sim32(m.grids[0], m.fb_phi, p, 0.f);
+      return f3(-s * bphi, c * bphi, bp);
+    }
+    default: return f3(0, 0, 0);
+  }
+}
+
+// ------------------------------------------------------- coefficients
+struct Coef32 {
+  float kI, kQ, kV, kF, kC, eI, eQ, eV;
+};
+
+// Kinematics of a (Gamma, v_hat) velocity for the LOS n (towards the
+// observer): Doppler factor D and the aberrated LOS n' (src/utils.cpp:147-162).
+__device__ __forceinline__ void kinematics32(float gamma, F3 vdir, F3 n, float& D, F3& nlp, float& beta) {
+  float g2 = gamma * gamma;
+  beta = sqrtf(fmaxf((gamma - 1.f) * (gamma + 1.f), 0.f)) / gamma;
+  F3 dv = vdir - n;
+  float one_m_bn = 1.f / (g2 * (1.f + beta)) + beta * 0.5f * fdot(dv, dv);
+  D = 1.f / (gamma * one_m_bn);
+  nlp = n * D - vdir * ((D + 1.f) * (gamma / (gamma + 1.f)) * beta);
+}
+
+template <bool FULL>
+__device__ __forceinline__ void coef32(const JshRequest& R, const JshFreqConst& F, F3 p, Coef32& c) {
+  const JshModel& m = R.model;
+  const JshMixed& X = R.mix;
+  float D, gamma, beta;
+  F3 nlp, vdir;
+  if (X.v_const) {
+    D = X.D;
+    gamma = X.gamma;
+    beta = X.beta;
+    nlp = f3(X.nlp[0], X.nlp[1], X.nlp[2]);
+    vdir = f3(0, 0, 1);
+  } else {
+    Vel v = vfield32(m, p);
+    gamma = v.gamma;
+    vdir = v.dir;
+    kinematics32(gamma, vdir, f3(X.nl[0], X.nl[1], X.nl[2]), D, nlp, beta);
+  }
+  float n = nfield32(m, p);
+  float np_ = m.n_plasma ? n : n / gamma;
+  if (m.b_scalar) {
+    float w = bscalar32(m, p) * D;
+    float P = fpow(w, X.pk);
+    float Rw = P * rsqrtf(w);
+    c.kI = F.ak * np_ * P;
+    c.eI = F.ae * np_ * Rw * D;
+    c.kQ = c.kV = c.kF = c.kC = c.eQ = c.eV = 0.f;
+    return;
+  }
+  F3 B = bvector32(m, p);
+  if (!m.b_plasma) {
+    // B' = B / Gamma + Gamma beta^2 / (1 + Gamma) v_hat (v_hat . B)
+    B = B * (1.f / gamma) + vdir * (gamma * beta * beta / (1.f + gamma) * fdot(vdir, B));
+  }
+  F3 cr = fcross(nlp, B);
+  float w = sqrtf(fdot(cr, cr)) * D;
+  float P = 0.f, Rw = 0.f;
+  if (w > 0.f) {
+    P = fpow(w, X.pk);
+    Rw = P * rsqrtf(w);
+  }
+  c.kI = F.ak * np_ * P;
+  c.eI = F.ae * np_ * Rw * D;
+  if (!FULL) return;
+  float bpar = fdot(B, nlp);
+  c.kQ = X.kq * c.kI;
+  c.eQ = X.eq * c.eI;
+  c.kV = -F.av * np_ * bpar * Rw * D;
+  c.eV = (w > 0.f) ? -F.aev * np_ * bpar * D * D * (P / w) : 0.f;
+  c.kF = F.af * np_ * bpar * D;
+  c.kC = -F.ac * np_ * (F.c1 * w * w - F.c2 * P);
+}
+
+}  // namespace jsh

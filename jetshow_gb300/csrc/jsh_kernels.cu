@@ -1,10 +1,10 @@
-// jsh_kernels.cu -- ray generation, hit/compaction and the static-schedule
-// FP64 transfer kernels, plus their launchers.  The mixed-precision and
-// persistent kernels are in jsh_persistent.cu.
+// jsh_kernels.cu -- ray generation, hit/compaction and inspection kernels
+// and the transfer dispatcher.  The FP64 transfer kernels are in
+// jsh_fp64.cu, the mixed-precision ones in jsh_persistent.cu.
 #include <cuda_runtime.h>
 
+#include "jsh_fields.cuh"
 #include "jsh_launch.h"
-#include "jsh_transfer64.cuh"
 
 using namespace jsh;
 
@@ -149,119 +149,16 @@ __global__ void grid_interp_kernel(JshGrid G, int field, const double* zr, int64
 
 }  // namespace
 
-// ------------------------------------------------------------ transfer
-namespace jsh {
 
-// Exclusive prefix of work items (n_hit * n_nu) over the batch, in shared memory.
-__device__ __forceinline__ void batch_prefix(const JshRequest* __restrict__ reqs, int n_req,
-                                             unsigned long long* base) {
-  if (threadIdx.x == 0) {
-    unsigned long long acc = 0;
-    for (int r = 0; r < n_req; ++r) {
-      base[r] = acc;
-      acc += (unsigned long long)(*reqs[r].n_hit) * (unsigned long long)reqs[r].n_nu;
-    }
-    base[n_req] = acc;
-  }
-  __syncthreads();
-}
 
-__device__ __forceinline__ int find_request(const unsigned long long* base, int n_req, unsigned long long w) {
-  int lo = 0, hi = n_req - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (base[mid] <= w) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
-__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Per-request device counters: warp-aggregated when the whole warp works on
-// one request, per-lane otherwise.
-__device__ __forceinline__ void add_counters(const JshRequest* __restrict__ reqs, int r, bool active,
-                                             unsigned long long evals, unsigned long long acc,
-                                             unsigned long long rej, unsigned status) {
-  int r0 = __shfl_sync(0xffffffffu, r, 0);
-  bool same = __all_sync(0xffffffffu, !active || r == r0);
-  bool any = __any_sync(0xffffffffu, active);
-  if (!any) return;
-  if (same) {
-    unsigned long long e = warp_sum(active ? evals : 0), a = warp_sum(active ? acc : 0),
-                       j = warp_sum(active ? rej : 0);
-    unsigned st = __reduce_or_sync(0xffffffffu, active ? status : 0u);
-    if ((threadIdx.x & 31) == 0) {
-      unsigned long long* c = reqs[r0].counters;
-      atomicAdd(&c[0], e);
-      atomicAdd(&c[1], a);
-      atomicAdd(&c[2], j);
-      atomicOr(&c[3], (unsigned long long)st);
-    }
-  } else if (active) {
-    unsigned long long* c = reqs[r].counters;
-    atomicAdd(&c[0], evals);
-    atomicAdd(&c[1], acc);
-    atomicAdd(&c[2], rej);
-    atomicOr(&c[3], (unsigned long long)status);
-  }
-}
-
-__device__ __forceinline__ void write_item(const JshRequest& R, int f, int64_t pix, const ItemOut& o) {
-  uint64_t q = (uint64_t)f * R.npix + (uint64_t)pix;
-  if (R.tau) R.tau[q] = o.tau;
-  if (R.l) R.l[q] = o.l;
-  if (R.I) R.I[q] = o.iquv[0];
-  if (R.Q) R.Q[q] = o.iquv[1];
-  if (R.U) R.U[q] = o.iquv[2];
-  if (R.V) R.V[q] = o.iquv[3];
-  if (R.status) R.status[q] = o.status;
-}
-
-}  // namespace jsh
-
-namespace {
-
-// One thread per (request, hit ray, frequency), all FP64.  Items are laid
-// out frequency-major within a request so adjacent lanes trace adjacent
-// pixels (similar path lengths, less divergence).
-__global__ void __launch_bounds__(128) transfer_static64_kernel(const JshRequest* __restrict__ reqs, int n_req) {
-  __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
-  batch_prefix(reqs, n_req, base);
-  unsigned long long w = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-  bool active = w < base[n_req];
-  int r = 0;
-  Ctl64 tot{0, 0, 0, 0, 0, 0, 0};
-  ItemOut o;
-  o.status = 0;
-  if (active) {
-    r = find_request(base, n_req, w);
-    const JshRequest& R = reqs[r];
-    unsigned long long local = w - base[r];
-    unsigned nhit = *R.n_hit;
-    int f = (int)(local / nhit);
-    unsigned h = (unsigned)(local % nhit);
-    const JshHit& H = R.hits[h];
-    if (R.P.full) transfer_item64<true>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
-    else transfer_item64<false>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
-    write_item(R, f, H.pix, o);
-  }
-  add_counters(reqs, r, active, tot.evals, tot.acc, tot.rej, o.status);
-}
-
-}  // namespace
-
-// Defined in jsh_persistent.cu.
-cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int schedule, bool full,
-                                      uint64_t max_items, const JshLaunchShape& shape, unsigned int* queue,
-                                      int num_sms, cudaStream_t stream);
+// Defined in jsh_fp64.cu and jsh_persistent.cu.
+cudaError_t jsh_launch_transfer_static64(const JshRequest* d_reqs, int n_req, uint64_t max_items, cudaStream_t stream);
 cudaError_t jsh_launch_transfer_persistent64(const JshRequest* d_reqs, int n_req, uint64_t max_items,
                                              const JshLaunchShape& shape, unsigned int* queue, int num_sms,
                                              cudaStream_t stream);
+cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int schedule, bool full,
+                                      uint64_t max_items, const JshLaunchShape& shape, unsigned int* queue,
+                                      int num_sms, cudaStream_t stream);
 
 cudaError_t jsh_launch_plane(const JshRequest* d_reqs, int n_req, uint64_t max_along, cudaStream_t stream) {
   if (n_req <= 0) return cudaSuccess;
@@ -288,10 +185,7 @@ cudaError_t jsh_launch_transfer(const JshRequest* d_reqs, int n_req, int precisi
     return jsh_launch_transfer_mixed(d_reqs, n_req, schedule, full, max_items, shape, queue, num_sms, stream);
   if (schedule == JSH_SCHED_PERSISTENT)
     return jsh_launch_transfer_persistent64(d_reqs, n_req, max_items, shape, queue, num_sms, stream);
-  const int bs = 128;
-  uint64_t blocks = (max_items + bs - 1) / bs;
-  transfer_static64_kernel<<<(unsigned)blocks, bs, 0, stream>>>(d_reqs, n_req);
-  return cudaGetLastError();
+  return jsh_launch_transfer_static64(d_reqs, n_req, max_items, stream);
 }
 
 cudaError_t jsh_launch_hit_rays(const JshModel& model, const double* d_orig, const double* d_dir, int64_t n,

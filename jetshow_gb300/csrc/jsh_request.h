@@ -21,8 +21,30 @@ struct JshParamsDev {
   int64_t max_steps;
 };
 
+// Mixed precision, one frequency: folded prefactors of the FP32 coefficient
+// algebra (see jsh_fields32.cuh), lengths in pc, intensities in units of
+// `scale`.
+struct JshFreqConst {
+  float ak, ae, av, aev, af, ac, c1, c2;
+  double scale;  // S: cgs intensity of one unit of the scaled state
+  double atol;   // I/IQUV-pass atol / S
+};
+
+// Mixed precision, per request.
+struct JshMixed {
+  int32_t v_const;       // ConstFlat velocity: Doppler factor and aberrated LOS are constants
+  float D, gamma, beta;  // of the constant velocity
+  float nlp[3];          // aberrated LOS of the constant velocity
+  float nl[3];           // LOS towards the observer (-ray direction)
+  float pk;              // (s + 2) / 2
+  float kq, eq;          // k_Q / k_I, eta_Q / eta_I
+  float reserved;
+  const JshFreqConst* fc;  // device [n_nu]
+};
+
 struct JshRequest {
   JshModel model;
+  JshMixed mix;
   JshPlane plane;
   JshParamsDev P;
   JshHit* hits;           // device [npix] (first n_hit valid)

@@ -38,6 +38,42 @@ constexpr double D1 = -12715105075.0 / 11282082432.0, D3 = 87487479700.0 / 32700
 constexpr int FAIL_LIMIT = 500;
 }  // namespace dp
 
+// Tableau rows of stages 2..7 (row 7 = the 5th-order weights b) and nodes.
+__device__ __forceinline__ double dp_a(int s, int j) {
+  switch (s * 8 + j) {
+    case 8: return dp::A21;
+    case 16: return dp::A31;
+    case 17: return dp::A32;
+    case 24: return dp::A41;
+    case 25: return dp::A42;
+    case 26: return dp::A43;
+    case 32: return dp::A51;
+    case 33: return dp::A52;
+    case 34: return dp::A53;
+    case 35: return dp::A54;
+    case 40: return dp::A61;
+    case 41: return dp::A62;
+    case 42: return dp::A63;
+    case 43: return dp::A64;
+    case 44: return dp::A65;
+    case 48: return dp::B1;
+    case 50: return dp::B3;
+    case 51: return dp::B4;
+    case 52: return dp::B5;
+    case 53: return dp::B6;
+    default: return 0.0;
+  }
+}
+__device__ __forceinline__ double dp_c(int s) {
+  switch (s) {
+    case 1: return dp::C2;
+    case 2: return dp::C3;
+    case 3: return dp::C4;
+    case 4: return dp::C5;
+    default: return 1.0;
+  }
+}
+
 __device__ __forceinline__ double dt_decrease(double dt, double err, double max_dt) {
   double f = 0.9 * pow(err, -1.0 / 3.0);
   dt *= (f > 0.2 ? f : 0.2);
@@ -109,30 +145,21 @@ __device__ uint32_t controlled_step64(const JshModel& m, const Path64& P, bool t
       if (++fails >= dp::FAIL_LIMIT) return JSH_ST_FAIL_LIMIT;
       continue;
     }
+    // stages 2..7 as a loop over the tableau (one right-hand-side call site);
+    // row 7 is the 5th-order solution, whose derivative is the FSAL stage
     double y[DIM], xn[DIM];
+#pragma unroll 1
+    for (int s = 1; s < 7; ++s) {
 #pragma unroll
-    for (int i = 0; i < DIM; ++i) y[i] = x[i] + dt * (dp::A21 * k[0][i]);
-    R::eval(m, P, tau, t + dp::C2 * dt, y, k[1]);
+      for (int i = 0; i < DIM; ++i) {
+        double acc = dp_a(s, 0) * k[0][i];
+        for (int j = 1; j < s; ++j) acc += dp_a(s, j) * k[j][i];
+        y[i] = x[i] + dt * acc;
+      }
+      R::eval(m, P, tau, t + dp_c(s) * dt, y, k[s]);
+    }
 #pragma unroll
-    for (int i = 0; i < DIM; ++i) y[i] = x[i] + dt * (dp::A31 * k[0][i] + dp::A32 * k[1][i]);
-    R::eval(m, P, tau, t + dp::C3 * dt, y, k[2]);
-#pragma unroll
-    for (int i = 0; i < DIM; ++i) y[i] = x[i] + dt * (dp::A41 * k[0][i] + dp::A42 * k[1][i] + dp::A43 * k[2][i]);
-    R::eval(m, P, tau, t + dp::C4 * dt, y, k[3]);
-#pragma unroll
-    for (int i = 0; i < DIM; ++i)
-      y[i] = x[i] + dt * (dp::A51 * k[0][i] + dp::A52 * k[1][i] + dp::A53 * k[2][i] + dp::A54 * k[3][i]);
-    R::eval(m, P, tau, t + dp::C5 * dt, y, k[4]);
-#pragma unroll
-    for (int i = 0; i < DIM; ++i)
-      y[i] = x[i] + dt * (dp::A61 * k[0][i] + dp::A62 * k[1][i] + dp::A63 * k[2][i] + dp::A64 * k[3][i] +
-                          dp::A65 * k[4][i]);
-    R::eval(m, P, tau, t + dt, y, k[5]);
-#pragma unroll
-    for (int i = 0; i < DIM; ++i)
-      xn[i] = x[i] + dt * (dp::B1 * k[0][i] + dp::B3 * k[2][i] + dp::B4 * k[3][i] + dp::B5 * k[4][i] +
-                           dp::B6 * k[5][i]);
-    R::eval(m, P, tau, t + dt, xn, k[6]);
+    for (int i = 0; i < DIM; ++i) xn[i] = y[i];
     C.evals += 6;
     double e = 0.0;
     bool bad = false;
