@@ -1,0 +1,314 @@
+"""Benchmark of the full-Stokes transfer path on one GB300.
+
+Workload (one step): the 512 x 1024 log-spaced conical jet at 8.1, 8.4, 12.1
+and 15.4 GHz, tau then IQUV at rtol 1e-6 / atol 1e-10, synthetic model of
+the configuration (no external data).  The metric counts (hit ray,
+frequency) work items per second.
+
+Forms timed in the same run:
+  * batched  -- mixed precision (FP32 stages / FP64 tau, Faraday angle and
+                step control), persistent refilling schedule: `value`;
+  * mixed    -- the same arithmetic, one thread per item (static schedule);
+  * plain    -- all-FP64, one thread per item (the plain GPU drop-in).
+`e2e` times the batched form through the C ABI with host buffers (outputs
+copied back to pinned host memory each step).  `--impl reference` times
+the CPU oracle (FP64 restatement of the reference's Observation::run with
+OpenMP over pixels) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import ctypes as C
+import io
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "full_stokes_rays_per_s"
+UNIT = "rays/s"
+WORKLOAD = "conical jet 512x1024 log-spaced (lg mas -3..-1), 4 freq (8.1/8.4/12.1/15.4 GHz), full Stokes, rtol 1e-6 atol 1e-10"
+# source-level op census of one mixed-precision full-Stokes right-hand-side
+# evaluation of this workload's model (ConstFlat V, helical conical B, BK n),
+# stage combination and error estimate amortised over the 6 evaluations of a
+# step: FP32 arithmetic instructions (an FMA counts once) and MUFU ops
+CENSUS_FP32_INSTR = 116
+CENSUS_MUFU = 14
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=int, default=1, help="shrink the image (debug only)")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.rows = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        for row in csv.reader(io.StringIO(out)):
+            if len(row) >= 9:
+                self.rows.append([x.strip() for x in row])
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def workload(scale):
+    from jetshow_gb300 import workloads as W
+    return W.conical_c1(scale=scale)
+
+
+def reference_arm(args):
+    """The CPU oracle (OpenMP over pixels, FP64) on a bounded sample."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from jetshow_gb300 import jet as J
+    from oracle import oracle as O
+    O.build()
+    jet, plane, nu, kw = workload(args.scale)
+    params = J.make_params(**kw)
+    threads = O.threads()
+    rng = np.random.default_rng(0)
+    # hit pixels of the plane (the oracle's own geometry)
+    o, d, _ = O.plane_rays(plane.desc())
+    nseg, _, _ = O.hit_rays(jet.desc(), o, np.tile(d, (o.shape[0], 1)))
+    hit = np.nonzero(nseg > 0)[0]
+    n_sample = min(hit.size, max(64, threads * 16))
+    vals = []
+    for step in range(args.warmup + args.steps):
+        pix = rng.choice(hit, size=n_sample, replace=False)
+        t0 = time.perf_counter()
+        O.render(jet.desc(), plane.desc(), nu, params, pix=pix, threads=threads)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            vals.append(n_sample * nu.size / dt)
+    v = float(np.mean(vals))
+    sample = f"{n_sample} random hit pixels x {nu.size} freq per step"
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * n_sample * nu.size / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD}, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(jet, plane, nu, kw, seconds=10.0):
+    from jetshow_gb300 import jet as J
+    from oracle import oracle as O
+    O.build()
+    params = J.make_params(**kw)
+    threads = O.threads()
+    o, d, _ = O.plane_rays(plane.desc())
+    nseg, _, _ = O.hit_rays(jet.desc(), o, np.tile(d, (o.shape[0], 1)))
+    hit = np.nonzero(nseg > 0)[0]
+    rng = np.random.default_rng(1)
+    n = min(hit.size, max(32, threads * 4))
+    total_items, total_t = 0, 0.0
+    while total_t < seconds and total_items < hit.size * nu.size:
+        pix = rng.choice(hit, size=n, replace=False)
+        t0 = time.perf_counter()
+        O.render(jet.desc(), plane.desc(), nu, params, pix=pix, threads=threads)
+        total_t += time.perf_counter() - t0
+        total_items += n * nu.size
+        n = min(hit.size, n * 2)
+    return {"value": total_items / total_t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{total_items} (hit pixel, freq) items drawn at random, {total_t:.1f} s"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from jetshow_gb300 import jet as J
+    from jetshow_gb300 import _capi as A
+    from jetshow_gb300.runtime import Context
+
+    ctx = Context(local)
+    jet, plane, nu, kw = workload(args.scale)
+    model, pdesc = jet.desc(), plane.desc()
+    na, nl = plane.image_size
+    npix = na * nl
+    stream = torch.cuda.Stream()
+    planes = {k: torch.zeros((nu.size, npix), dtype=torch.float64, device="cuda") for k in
+              ("tau", "l", "I", "Q", "U", "V")}
+    planes["status"] = torch.zeros((nu.size, npix), dtype=torch.int32, device="cuda")
+    ptrs = {k: v.data_ptr() for k, v in planes.items()}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(params, steps, warmup):
+        ms = []
+        for i in range(warmup + steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                ctx.render_device(model, pdesc, nu, params, stream.cuda_stream, ptrs)
+                e1.record(stream)
+            stream.synchronize()
+            if i >= warmup:
+                ms.append(e0.elapsed_time(e1))
+        return ms, ctx.last_stats()
+
+    p_batched = J.make_params(precision="mixed", schedule="persistent", **kw)
+    p_mixed = J.make_params(precision="mixed", schedule="static", **kw)
+    p_plain = J.make_params(precision="fp64", schedule="static", **kw)
+
+    # ---- batched form (headline), clocks sampled during the timed steps
+    barrier()
+    with ClockSampler(local) as clk:
+        ms_b, st_b = timed(p_batched, args.steps, args.warmup)
+    barrier()
+    items = st_b["n_work_items"]
+    out_b = {k: v.cpu().numpy() for k, v in planes.items()}
+    t_step = float(np.mean(ms_b))
+    if world > 1:
+        tt = torch.tensor([max(ms_b)], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    value = items * world / (t_step * 1e-3)
+
+    # ---- static mixed and plain FP64 forms
+    ms_m, st_m = timed(p_mixed, min(args.steps, 3), 1)
+    mixed_rate = st_m["n_work_items"] / (np.mean(ms_m) * 1e-3)
+    plain_rate, rel = None, {}
+    if not args.no_plain:
+        ms_p, st_p = timed(p_plain, 1, 1)
+        plain_rate = st_p["n_work_items"] / (np.mean(ms_p) * 1e-3)
+        out_p = {k: v.cpu().numpy() for k, v in planes.items()}
+        hit = (out_p["status"] & 1) != 0
+        for f in range(nu.size):
+            Ip, Ib = out_p["I"][f], out_b["I"][f]
+            imax = np.abs(Ip).max()
+            sel = np.abs(Ip) > 1e-6 * imax
+            rel["I"] = max(rel.get("I", 0.0), float(np.max(np.abs(Ib[sel] - Ip[sel]) / np.abs(Ip[sel]))))
+            for k in ("Q", "U", "V"):
+                rel[k] = max(rel.get(k, 0.0), float(np.max(np.abs(out_b[k][f] - out_p[k][f])) / imax))
+            rel["flux"] = max(rel.get("flux", 0.0), float(abs(Ib.sum() - Ip.sum()) / abs(Ip.sum())))
+        notx = hit & (out_p["tau"] < kw["tau_max"]) & (out_b["tau"] < kw["tau_max"])
+        rel["tau"] = float(np.max(np.abs(out_b["tau"][notx] - out_p["tau"][notx]) / np.abs(out_p["tau"][notx])))
+
+    # ---- end to end through the C ABI with pinned host buffers
+    host = {k: torch.empty((nu.size, npix), dtype=torch.float64, pin_memory=True) for k in
+            ("tau", "l", "I", "Q", "U", "V")}
+    host["status"] = torch.empty((nu.size, npix), dtype=torch.int32, pin_memory=True)
+    img = A.Image(*(C.cast(host[k].data_ptr(), C.POINTER(C.c_double)) for k in ("tau", "l", "I", "Q", "U", "V")),
+                  C.cast(host["status"].data_ptr(), C.POINTER(C.c_uint32)))
+    st = A.Stats()
+    nu_c = np.ascontiguousarray(nu, dtype=np.float64)
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = ctx.lib.jsh_observation_run(ctx.handle, C.byref(model), C.byref(pdesc), A.dptr(nu_c), nu_c.size,
+                                         C.byref(p_batched), C.byref(img), C.byref(st))
+        t1 = time.perf_counter()
+        assert rc == 0, ctx.lib.jsh_last_error()
+        if i >= args.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+    e2e_value = st.n_work_items * world / (np.mean(e2e_ms) * 1e-3)
+    d2h = sum(v.numel() * v.element_size() for v in host.values())
+    h2d = C.sizeof(A.ModelDesc) + C.sizeof(A.PlaneDesc) + C.sizeof(A.Params) + nu_c.nbytes
+
+    # ---- roofline of the dominant kernel (persistent transfer)
+    peaks = ctx.device_peaks()
+    evals_per_s = st_b["rhs_evals"] / (t_step * 1e-3)
+    achieved = evals_per_s * CENSUS_FP32_INSTR * 2 / 1e12
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
+            "frac": achieved / peaks["fp32_tflops"], "traffic": None,
+            "peak_source": "measured FMA-chain microbenchmark on this GPU in this run (MEASURED_PEAKS.json "
+                           "holds only HBM and bf16 peaks)",
+            "census": {"fp32_instr_per_rhs": CENSUS_FP32_INSTR, "mufu_per_rhs": CENSUS_MUFU},
+            "rhs_evals_per_s": evals_per_s,
+            "mufu": {"achieved_tops": evals_per_s * CENSUS_MUFU / 1e12, "peak_tops": peaks["mufu_tops"],
+                     "frac": evals_per_s * CENSUS_MUFU / 1e12 / peaks["mufu_tops"]},
+            "fp64_peak_tflops": peaks["fp64_tflops"]}
+    cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 else None
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "image": [na, nl], "n_freq": int(nu.size),
+                           "work_items": int(items), "l2": "256 MB buffer written between timed steps",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "forms": {"batched_rays_per_s": value, "mixed_static_rays_per_s": mixed_rate,
+                          "plain_fp64_rays_per_s": plain_rate,
+                          "batched_over_plain": (value / plain_rate) if plain_rate else None},
+                "rel_err_vs_plain_fp64": rel,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "ms_per_step": float(np.mean(e2e_ms))},
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": 4, "rhs_evals_per_step": st_b["rhs_evals"],
+                "steps_accepted": st_b["steps_accepted"], "steps_rejected": st_b["steps_rejected"]}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

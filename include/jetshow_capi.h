@@ -360,6 +360,14 @@ int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model,
                  const jsh_plane_desc* plane, const double* nu_hz,
                  int32_t n_nu, const jsh_params* params, jsh_tuning* best);
 
+/* --------------------------------------------------------- diagnostics */
+/* Measured issue rates of the context's device, for roofline fractions of
+ * the compute-bound transfer kernels: FP32 FMA throughput (TFLOP/s, two
+ * flops per FMA), MUFU ex2 throughput (T ops/s) and FP64 FMA throughput
+ * (TFLOP/s), each from a dependent-chain microbenchmark over every SM.
+ * No reference counterpart (the reference has no device code). */
+int jsh_device_peaks(jsh_ctx* ctx, double* fp32_tflops, double* mufu_tops, double* fp64_tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -253,6 +253,7 @@ SIGNATURES = [
     ("jsh_server_wait", C.c_int,
      [C.c_void_p, C.c_uint64, C.c_int32, _P(Image), _P(RequestStats)]),
     ("jsh_server_cancel", C.c_int, [C.c_void_p, C.c_uint64]),
+    ("jsh_device_peaks", C.c_int, [C.c_void_p, _D, _D, _D]),
     ("jsh_autotune", C.c_int,
      [C.c_void_p, _P(ModelDesc), _P(PlaneDesc), _D, C.c_int32, _P(Params), _P(Tuning)]),
 ]

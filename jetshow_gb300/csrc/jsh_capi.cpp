@@ -546,3 +546,17 @@ extern "C" int jsh_hit_rays(jsh_ctx* ctx, const jsh_model_desc* model, const dou
   JSH_CUDA_TRY(cudaStreamSynchronize(s));
   return JSH_OK;
 }
+
+cudaError_t jsh_run_peaks(int num_sms, double* fp32_tflops, double* mufu_tops, double* fp64_tflops,
+                          cudaStream_t stream);
+
+extern "C" int jsh_device_peaks(jsh_ctx* ctx, double* fp32_tflops, double* mufu_tops, double* fp64_tflops) {
+  if (!ctx) {
+    jsh_set_error("null context");
+    return JSH_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  JSH_CUDA_TRY(cudaSetDevice(ctx->device));
+  JSH_CUDA_TRY(jsh_run_peaks(ctx->num_sms, fp32_tflops, mufu_tops, fp64_tflops, ctx->stream));
+  return JSH_OK;
+}

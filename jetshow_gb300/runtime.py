@@ -74,6 +74,12 @@ class Context:
         check(self.lib, self.lib.jsh_last_stats(self.handle, C.byref(st)))
         return stats_dict(st)
 
+    def device_peaks(self):
+        """Measured FP32 TFLOP/s, MUFU ex2 T ops/s and FP64 TFLOP/s of the device."""
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        check(self.lib, self.lib.jsh_device_peaks(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return {"fp32_tflops": a.value, "mufu_tops": b.value, "fp64_tflops": c.value}
+
     # ----------------------------------------------------- inspection
     def plane_rays(self, plane: A.PlaneDesc):
         n = int(plane.n_across * plane.n_along)
