@@ -147,9 +147,89 @@ __global__ void grid_interp_kernel(JshGrid G, int field, const double* zr, int64
   out[i] = grid_value(G, field, zr[2 * i], zr[2 * i + 1], nan_value);
 }
 
+// Throughput microbenchmarks: 8 independent dependent chains per thread.
+__global__ void peak_fp32_kernel(float* out, int iters, float a) {
+  float v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = threadIdx.x * 1e-3f + i;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = fmaf(v[i], a, 1e-7f);
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += v[i];
+  if (s == 12345.f) out[0] = s;
+}
+
+__global__ void peak_mufu_kernel(float* out, int iters) {
+  float v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = threadIdx.x * 1e-6f + i * 1e-3f;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      float r;
+      asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v[i]));
+      v[i] = r * 1e-3f;
+    }
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += v[i];
+  if (s == 12345.f) out[0] = s;
+}
+
+__global__ void peak_fp64_kernel(double* out, int iters, double a) {
+  double v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = threadIdx.x * 1e-3 + i;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = fma(v[i], a, 1e-7);
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += v[i];
+  if (s == 12345.0) out[0] = s;
+}
+
 }  // namespace
 
-
+cudaError_t jsh_run_peaks(int num_sms, double* fp32_tflops, double* mufu_tops, double* fp64_tflops,
+                          cudaStream_t stream) {
+  void* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, 64);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const int bs = 256, blocks = num_sms * 8;
+  const double threads = (double)bs * blocks;
+  const int it32 = 40000, itm = 8000, it64 = 2000;
+  float ms = 0.f;
+  peak_fp32_kernel<<<blocks, bs, 0, stream>>>((float*)buf, it32 / 2, 0.999999f);  // clocks up
+  cudaEventRecord(a, stream);
+  peak_fp32_kernel<<<blocks, bs, 0, stream>>>((float*)buf, it32, 0.999999f);
+  cudaEventRecord(b, stream);
+  cudaEventSynchronize(b);
+  cudaEventElapsedTime(&ms, a, b);
+  if (fp32_tflops) *fp32_tflops = threads * it32 * 8 * 2 / (ms * 1e-3) / 1e12;
+  cudaEventRecord(a, stream);
+  peak_mufu_kernel<<<blocks, bs, 0, stream>>>((float*)buf, itm);
+  cudaEventRecord(b, stream);
+  cudaEventSynchronize(b);
+  cudaEventElapsedTime(&ms, a, b);
+  if (mufu_tops) *mufu_tops = threads * itm * 8 / (ms * 1e-3) / 1e12;
+  cudaEventRecord(a, stream);
+  peak_fp64_kernel<<<blocks, bs, 0, stream>>>((double*)buf, it64, 0.999999);
+  cudaEventRecord(b, stream);
+  cudaEventSynchronize(b);
+  cudaEventElapsedTime(&ms, a, b);
+  if (fp64_tflops) *fp64_tflops = threads * it64 * 8 * 2 / (ms * 1e-3) / 1e12;
+  e = cudaGetLastError();
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  return e;
+}
 
 // Defined in jsh_fp64.cu and jsh_persistent.cu.
 cudaError_t jsh_launch_transfer_static64(const JshRequest* d_reqs, int n_req, uint64_t max_items, cudaStream_t stream);
