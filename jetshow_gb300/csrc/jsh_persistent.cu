@@ -181,7 +181,7 @@ __device__ __forceinline__ void rhs32(const JshRequest& R, const JshFreqConst& F
 // warp_tau: every active lane of the warp is in its tau pass, so only k_I
 // is evaluated.
 template <bool FULL>
-__device__ __noinline__ void lane_step(Lane& L, const JshRequest* __restrict__ reqs, bool warp_tau) {
+__device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict__ reqs, bool warp_tau) {
   constexpr int NK = FULL ? 5 : 1;
   const JshRequest& R = reqs[L.r];
   const JshFreqConst F = R.mix.fc[L.f];
@@ -190,9 +190,10 @@ __device__ __noinline__ void lane_step(Lane& L, const JshRequest* __restrict__ r
   const double sgn = tau ? 1.0 : -1.0;
   const double ddx = sgn * R.plane.dx, ddy = sgn * R.plane.dy, ddz = sgn * R.plane.dz;
   const F3 dirf = f3((float)ddx, (float)ddy, (float)ddz);
-  const double max_dt = tau ? R.P.dt_max * INV_PC : 0.0;
-  const double atol = tau ? R.P.tau_atol : F.atol;
-  const double rtol = tau ? R.P.tau_rtol : R.P.rtol;
+  const double max_dt = tau ? R.mix.dt_max_pc : 0.0;
+  // error-norm tolerances in FP32 (the norm needs a few digits; t and dt stay FP64)
+  const float atol = tau ? (float)R.P.tau_atol : (float)F.atol;
+  const float rtol = tau ? (float)R.P.tau_rtol : (float)R.P.rtol;
 
   // integrate_adaptive / adaptive range: finish at exactly t = length
   if (!(L.length - L.t > DBL_EPSILON)) goto segment_done;
@@ -212,9 +213,14 @@ __device__ __noinline__ void lane_step(Lane& L, const JshRequest* __restrict__ r
   }
   {
     const F3 pn = f3((float)(L.p0x + L.t * ddx), (float)(L.p0y + L.t * ddy), (float)(L.p0z + L.t * ddz));
-    double cn = 1.0, sn = 0.0;
-    if (FULL && !tau) sincos(fmod(L.chi, 6.283185307179586), &sn, &cn);
-    const float c0 = (float)cn, s0 = (float)sn;
+    // rotation of the frame at the step start: chi reduced modulo 2 pi in FP64
+    // (3 FP64 operations), then an FP32 sincos of the reduced angle
+    float c0 = 1.f, s0 = 0.f;
+    if (FULL && !tau) {
+      const double two_pi = 6.283185307179586;
+      const float chr = (float)fma(-two_pi, rint(L.chi * (1.0 / two_pi)), L.chi);
+      sincosf(chr, &s0, &c0);
+    }
     if (!L.init) {
       rhs32<FULL>(R, F, tau, coef_tau_only, pn, L.x, c0, s0, L.k1);
       L.evals++;
@@ -270,30 +276,29 @@ __device__ __noinline__ void lane_step(Lane& L, const JshRequest* __restrict__ r
       err[c] = h * ((float)dp::E1 * k[0][c] + (float)dp::E3 * k[2][c] + (float)dp::E4 * k[3][c] +
                     (float)dp::E5 * k[4][c] + (float)dp::E6 * k[5][c] + (float)dp::E7 * k[6][c]);
     }
-    // odeint default error checker, FP64 denominators
-    const double adt = fabs(L.dt);
-    double e;
+    // odeint default error checker: max_i |err_i| / (atol + rtol (|x_i| + |dt| |x'_i|))
+    const float adt = fabsf(h);
+    float e;
     if (tau) {
-      e = fabs((double)err[0]) / (atol + rtol * (fabs(L.tau_seg) + adt * fabs((double)k[0][0])));
+      e = fabsf(err[0]) / fmaf(rtol, fmaf(adt, fabsf(k[0][0]), fabsf((float)L.tau_seg)), atol);
     } else {
-      e = 0.0;
+      e = 0.f;
 #pragma unroll
       for (int c = 0; c < (FULL ? 4 : 1); ++c) {
-        double r = fabs((double)err[c]) / (atol + rtol * (fabs((double)L.x[c]) + adt * fabs((double)k[0][c])));
-        e = r > e ? r : e;
+        float r = fabsf(err[c]) / fmaf(rtol, fmaf(adt, fabsf(k[0][c]), fabsf(L.x[c])), atol);
+        e = fmaxf(e, r);
       }
       if (FULL) {
-        double P = sqrt((double)L.x[1] * L.x[1] + (double)L.x[2] * L.x[2]);
-        double r = fabs((double)err[NK - 1]) * P / (atol + rtol * P);
-        e = r > e ? r : e;
+        float P = sqrtf(fmaf(L.x[1], L.x[1], L.x[2] * L.x[2]));
+        e = fmaxf(e, fabsf(err[NK - 1]) * P / fmaf(rtol, P, atol));
       }
     }
     if (!(e == e) || isinf(e)) {
       L.status |= JSH_ST_NAN;
       goto abort;
     }
-    if (e > 1.0) {
-      float f = 0.9f * __powf((float)e, -1.0f / 3.0f);
+    if (e > 1.0f) {
+      float f = 0.9f * __powf(e, -1.0f / 3.0f);
       L.dt *= (double)(f > 0.2f ? f : 0.2f);
       if (max_dt != 0.0 && fabs(L.dt) > max_dt) L.dt = max_dt;
       L.rej++;
@@ -313,8 +318,8 @@ __device__ __noinline__ void lane_step(Lane& L, const JshRequest* __restrict__ r
     L.t = t_new;
     L.fails = 0;
     L.acc++;
-    if (e < 0.5) {
-      float ee = (float)e > 0.00032f ? (float)e : 0.00032f;
+    if (e < 0.5f) {
+      float ee = e > 0.00032f ? e : 0.00032f;
       L.dt *= (double)(0.9f * __powf(ee, -0.2f));
       if (max_dt != 0.0 && fabs(L.dt) > max_dt) L.dt = max_dt;
     }
@@ -509,6 +514,7 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   X.nl[1] = (float)ny;
   X.nl[2] = (float)nz;
   X.pk = (float)((s + 2.) / 2.);
+  X.dt_max_pc = req->P.dt_max / JSH_PC;
   X.kq = (float)m.kq_ratio;
   X.eq = (float)m.eq_ratio;
   if (m.v_kind == JSH_V_CONST_FLAT) {

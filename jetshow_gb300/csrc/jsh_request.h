@@ -39,6 +39,7 @@ struct JshMixed {
   float pk;              // (s + 2) / 2
   float kq, eq;          // k_Q / k_I, eta_Q / eta_I
   float reserved;
+  double dt_max_pc;      // tau-pass step limit [pc], 0 = none
   const JshFreqConst* fc;  // device [n_nu]
 };
 
