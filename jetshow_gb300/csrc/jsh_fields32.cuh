@@ -244,8 +244,8 @@ __device__ __forceinline__ void kinematics32(float gamma, F3 vdir, F3 n, float& 
   nlp = n * D - vdir * ((D + 1.f) * (gamma / (gamma + 1.f)) * beta);
 }
 
-template <bool FULL>
-__device__ __forceinline__ void coef32(const JshRequest& R, const JshFreqConst& F, F3 p, Coef32& c) {
+__device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqConst& F, F3 p, bool full, Coef32& c) {
+
   const JshModel& m = R.model;
   const JshMixed& X = R.mix;
   float D, gamma, beta;
@@ -287,7 +287,7 @@ __device__ __forceinline__ void coef32(const JshRequest& R, const JshFreqConst& 
   }
   c.kI = F.ak * np_ * P;
   c.eI = F.ae * np_ * Rw * D;
-  if (!FULL) return;
+  if (!full) return;
   float bpar = fdot(B, nlp);
   c.kQ = X.kq * c.kI;
   c.eQ = X.eq * c.eI;

@@ -1,10 +1,9 @@
 // jsh_persistent.cu -- the mixed-precision transfer: FP32 right-hand sides
-// and Runge-Kutta stages; FP64 time, step size, error-control arithmetic,
-// accumulated optical depth and Faraday rotation angle.  One work item is a
-// (request, hit ray, frequency); its tau pass (src/Observation.cpp:126-214)
-// and I/IQUV pass (src/Observation.cpp:242-308, src/System.cpp:41-63) run
-// as a per-lane state machine that advances by one Dormand-Prince attempt
-// per call, so that
+// and Runge-Kutta stages; FP64 time, step size, accumulated optical depth
+// and Faraday rotation angle.  One work item is a (request, hit ray,
+// frequency); its tau pass (src/Observation.cpp:126-214) and I/IQUV pass
+// (src/Observation.cpp:242-308, src/System.cpp:41-63) run as a per-lane
+// state machine that advances by one Dormand-Prince attempt per call, so that
 //  * the static schedule runs one item per thread to completion, and
 //  * the persistent schedule keeps every warp busy: lanes whose ray has
 //    finished are refilled from a global work queue (warp ballot + popc
@@ -21,6 +20,12 @@
 // error norm adds |err_chi| * |P| as the polarised-intensity error of the
 // rotation.  Intensities are scaled by a per-frequency power of two and
 // lengths are in pc so the FP32 state stays well inside its range.
+//
+// Code size matters as much as arithmetic here: the stages run as a rolled
+// loop over a __constant__ tableau with the stage derivatives in shared
+// memory, so the coefficient code exists once per kernel and the kernel
+// fits the SM instruction caches even when the lanes of a warp are in
+// different phases.
 #include <float.h>
 #include <math.h>
 
@@ -37,6 +42,22 @@ namespace {
 
 constexpr uint8_t PH_IDLE = 0, PH_TAU = 1, PH_IQUV = 2;
 constexpr double INV_PC = 1.0 / JSH_PC;
+
+// Dormand-Prince tableau in FP32: rows 1..6 of a (row 6 = the 5th-order
+// weights b), nodes c, error weights e = b - b_hat, dense-output weights d.
+__constant__ float c_A[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {(float)dp::A21, 0, 0, 0, 0, 0},
+    {(float)dp::A31, (float)dp::A32, 0, 0, 0, 0},
+    {(float)dp::A41, (float)dp::A42, (float)dp::A43, 0, 0, 0},
+    {(float)dp::A51, (float)dp::A52, (float)dp::A53, (float)dp::A54, 0, 0},
+    {(float)dp::A61, (float)dp::A62, (float)dp::A63, (float)dp::A64, (float)dp::A65, 0},
+    {(float)dp::B1, 0, (float)dp::B3, (float)dp::B4, (float)dp::B5, (float)dp::B6}};
+__constant__ float c_C[7] = {0, (float)dp::C2, (float)dp::C3, (float)dp::C4, (float)dp::C5, 1.f, 1.f};
+__constant__ float c_E[7] = {(float)dp::E1, 0, (float)dp::E3, (float)dp::E4, (float)dp::E5, (float)dp::E6,
+                             (float)dp::E7};
+__constant__ float c_D[7] = {(float)dp::D1, 0, (float)dp::D3, (float)dp::D4, (float)dp::D5, (float)dp::D6,
+                             (float)dp::D7};
 
 struct Lane {
   int r, f;
@@ -58,9 +79,25 @@ struct Lane {
   uint32_t evals, acc, rej;
 };
 
+// Stage derivatives of this thread: shared[(s * NK + c) * blockDim + tid].
+template <int NK>
+struct Stages {
+  float* sh;
+  __device__ __forceinline__ float& operator()(int s, int c) const {
+    return sh[(s * NK + c) * blockDim.x + threadIdx.x];
+  }
+};
+
 __device__ __forceinline__ double seg_len_cm(const JshHit& H, int s, double ox, double oy, double oz) {
   double dx = ox - H.seg[s][0], dy = oy - H.seg[s][1], dz = oz - H.seg[s][2];
   return sqrt((dx * dx + dy * dy) + dz * dz);
+}
+
+__device__ __noinline__ double first_step_divisor(double tau_bg, int n) {
+  // auto_n of src/Observation.cpp:254-258
+  double auto_n = n;
+  if (tau_bg > 0.1) auto_n = steps_schedule(tau_bg, n, 10 * n);
+  return auto_n;
 }
 
 __device__ __forceinline__ void begin_tau_segment(Lane& L, const JshRequest& R, const JshHit& H) {
@@ -92,10 +129,8 @@ __device__ __forceinline__ void begin_iquv_segment(Lane& L, const JshRequest& R,
   L.p0x = ox * INV_PC;
   L.p0y = oy * INV_PC;
   L.p0z = oz * INV_PC;
-  double auto_n = R.P.n;
-  if (L.tau_bg > 0.1) auto_n = steps_schedule(L.tau_bg, R.P.n, 10 * R.P.n);
   L.t = 0.0;
-  L.dt = L.length / auto_n;
+  L.dt = L.length / first_step_divisor(L.tau_bg, R.P.n);
   L.init = false;
   L.nsteps = 0;
   L.fails = 0;
@@ -125,45 +160,75 @@ __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict
   begin_tau_segment(L, R, H);
 }
 
-__device__ __forceinline__ void lane_finish(Lane& L, const JshRequest* __restrict__ reqs) {
-  const JshRequest& R = reqs[L.r];
-  const JshHit& H = R.hits[L.h];
-  const JshFreqConst& F = R.mix.fc[L.f];
-  uint64_t q = (uint64_t)L.f * R.npix + (uint64_t)H.pix;
-  double S = F.scale;
+// Writes one finished item (the Stokes vector rotated back to the lab frame
+// in FP64) and its counters.
+__device__ __noinline__ void write_finished(const JshRequest* __restrict__ reqs, int r, int f, uint32_t h,
+                                            double tau_bg, double thick, double chi, float x0, float x1, float x2,
+                                            float x3, uint32_t status, uint32_t evals, uint32_t acc,
+                                            uint32_t rej) {
+  const JshRequest& R = reqs[r];
+  const JshHit& H = R.hits[h];
+  uint64_t q = (uint64_t)f * R.npix + (uint64_t)H.pix;
+  double S = R.mix.fc[f].scale;
   double sc, ss;
-  sincos(L.chi, &ss, &sc);
-  double qq = L.x[1], uu = L.x[2];
-  if (R.tau) R.tau[q] = L.tau_bg;
-  if (R.l) R.l[q] = L.thick;
-  if (R.I) R.I[q] = S * (double)L.x[0];
+  sincos(chi, &ss, &sc);
+  double qq = x1, uu = x2;
+  if (R.tau) R.tau[q] = tau_bg;
+  if (R.l) R.l[q] = thick;
+  if (R.I) R.I[q] = S * (double)x0;
   if (R.Q) R.Q[q] = S * (sc * qq - ss * uu);
   if (R.U) R.U[q] = S * (ss * qq + sc * uu);
-  if (R.V) R.V[q] = S * (double)L.x[3];
-  if (R.status) R.status[q] = L.status;
+  if (R.V) R.V[q] = S * (double)x3;
+  if (R.status) R.status[q] = status;
   unsigned long long* c = R.counters;
-  atomicAdd(&c[0], (unsigned long long)L.evals);
-  atomicAdd(&c[1], (unsigned long long)L.acc);
-  atomicAdd(&c[2], (unsigned long long)L.rej);
-  atomicOr(&c[3], (unsigned long long)L.status);
+  atomicAdd(&c[0], (unsigned long long)evals);
+  atomicAdd(&c[1], (unsigned long long)acc);
+  atomicAdd(&c[2], (unsigned long long)rej);
+  atomicOr(&c[3], (unsigned long long)status);
+}
+
+__device__ __forceinline__ void lane_finish(Lane& L, const JshRequest* __restrict__ reqs) {
+  write_finished(reqs, L.r, L.f, L.h, L.tau_bg, L.thick, L.chi, L.x[0], L.x[1], L.x[2], L.x[3], L.status, L.evals,
+                 L.acc, L.rej);
   L.phase = PH_IDLE;
 }
 
-// Right-hand side at a stage.  tau: dk[0] = k_I.  IQUV: the rotating-frame
-// system above; dk[4] = k_F = dchi/dt.
-template <bool FULL>
-__device__ __forceinline__ void rhs32(const JshRequest& R, const JshFreqConst& F, bool tau, bool tau_coef_only,
-                                      F3 p, const float* y, float cs, float sn, float* dk) {
+// Bisection for the tau_max crossing on the dense output of the last step
+// (src/Observation.cpp:166-190); returns the crossing time [pc].
+__device__ __noinline__ double crossing_time(double tau_old, double t_old, double dt_used, float h, float k1,
+                                             float k3, float k4, float k5, float k6, float k7, float inc,
+                                             double tau_max, double tau_prec) {
+  const float ydiff = inc;
+  const float bspl = h * k1 - ydiff;
+  const float r4 = ydiff - h * k7 - bspl;
+  const float r5 = h * (c_D[0] * k1 + c_D[2] * k3 + c_D[3] * k4 + c_D[4] * k5 + c_D[5] * k6 + c_D[6] * k7);
+  double t0 = t_old, t1 = t_old + dt_used, xm = tau_old + (double)inc, tm;
+  int it = 0;
+  while (fabs(xm - tau_max) > tau_prec) {
+    if (++it > 200) return -1.0;  // no convergence: the caller flags JSH_ST_BISECT_LIMIT
+    tm = 0.5 * (t0 + t1);
+    float th = (float)((tm - t_old) / dt_used), th1 = 1.f - th;
+    xm = tau_old + (double)(th * (ydiff + th1 * (bspl + th * (r4 + th1 * r5))));
+    if (xm > tau_max) t1 = tm;
+    else t0 = tm;
+  }
+  return 0.5 * (t0 + t1);
+}
+
+// Coefficients (one call site per kernel); `full` = false stops after
+// k_I, eta_I (the tau pass, or I-only output).
+__device__ __forceinline__ void rhs32(const JshRequest& R, const JshFreqConst& F, bool tau, bool full, F3 p,
+                                      const float* y, float cs, float sn, float* dk) {
   Coef32 c;
-  if (tau_coef_only || !FULL) coef32<false>(R, F, p, c);
-  else coef32<true>(R, F, p, c);
+  coef32_rt(R, F, p, full, c);
   if (tau) {
     dk[0] = c.kI;
-    if (FULL) dk[1] = dk[2] = dk[3] = dk[4] = 0.f;
+    dk[1] = dk[2] = dk[3] = dk[4] = 0.f;
     return;
   }
-  if (!FULL) {
+  if (!full) {
     dk[0] = c.eI - c.kI * y[0];
+    dk[1] = dk[2] = dk[3] = dk[4] = 0.f;
     return;
   }
   float Qlab = cs * y[1] - sn * y[2];
@@ -181,12 +246,14 @@ __device__ __forceinline__ void rhs32(const JshRequest& R, const JshFreqConst& F
 // warp_tau: every active lane of the warp is in its tau pass, so only k_I
 // is evaluated.
 template <bool FULL>
-__device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict__ reqs, bool warp_tau) {
+__device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict__ reqs, bool warp_tau,
+                                          const Stages<FULL ? 5 : 1>& K) {
   constexpr int NK = FULL ? 5 : 1;
+  constexpr int NX = FULL ? 4 : 1;
   const JshRequest& R = reqs[L.r];
   const JshFreqConst F = R.mix.fc[L.f];
   const bool tau = (L.phase == PH_TAU);
-  const bool coef_tau_only = tau && warp_tau;
+  const bool coef_full = FULL && !(tau && warp_tau);
   const double sgn = tau ? 1.0 : -1.0;
   const double ddx = sgn * R.plane.dx, ddy = sgn * R.plane.dy, ddz = sgn * R.plane.dz;
   const F3 dirf = f3((float)ddx, (float)ddy, (float)ddz);
@@ -213,7 +280,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
   }
   {
     const F3 pn = f3((float)(L.p0x + L.t * ddx), (float)(L.p0y + L.t * ddy), (float)(L.p0z + L.t * ddz));
-    // rotation of the frame at the step start: chi reduced modulo 2 pi in FP64
+    // frame rotation at the step start: chi reduced modulo 2 pi in FP64
     // (3 FP64 operations), then an FP32 sincos of the reduced angle
     float c0 = 1.f, s0 = 0.f;
     if (FULL && !tau) {
@@ -221,71 +288,66 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       const float chr = (float)fma(-two_pi, rint(L.chi * (1.0 / two_pi)), L.chi);
       sincosf(chr, &s0, &c0);
     }
+    const float h = (float)L.dt;
+    float dk[5];
     if (!L.init) {
-      rhs32<FULL>(R, F, tau, coef_tau_only, pn, L.x, c0, s0, L.k1);
+      rhs32(R, F, tau, coef_full, pn, L.x, c0, s0, dk);
+#pragma unroll
+      for (int c = 0; c < NK; ++c) L.k1[c] = dk[c];
       L.evals++;
       L.init = true;
     }
-    const float h = (float)L.dt;
-    float k[7][NK];
 #pragma unroll
-    for (int c = 0; c < NK; ++c) k[0][c] = L.k1[c];
-    float y[4];
-    auto stage = [&](int i, float cfrac, const float* a) {
-      // y = x + h * sum_j a_j k_j ; rotation increment from the k_F column
+    for (int c = 0; c < NK; ++c) K(0, c) = L.k1[c];
+    float inc[NK];
+#pragma unroll 1
+    for (int s = 1; s < 7; ++s) {
+      float acc[NK];
 #pragma unroll
-      for (int c = 0; c < (FULL ? 4 : 1); ++c) {
-        float acc = 0.f;
+      for (int c = 0; c < NK; ++c) acc[c] = 0.f;
+      for (int j = 0; j < s; ++j) {
+        const float a = c_A[s][j];
 #pragma unroll
-        for (int j = 0; j < 6; ++j)
-          if (j < i) acc = fmaf(a[j], k[j][c], acc);
-        y[c] = fmaf(h, acc, L.x[c]);
+        for (int c = 0; c < NK; ++c) acc[c] = fmaf(a, K(j, c), acc[c]);
       }
-      float cs = c0, sn2 = s0;
+      float y[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) y[c] = (c < NX) ? fmaf(h, acc[c < NK ? c : 0], L.x[c]) : 0.f;
+      float cs = c0, sn = s0;
       if (FULL && !tau) {
-        float d = 0.f;
-#pragma unroll
-        for (int j = 0; j < 6; ++j)
-          if (j < i) d = fmaf(a[j], k[j][NK - 1], d);
         float sd, cd;
-        __sincosf(h * d, &sd, &cd);
+        __sincosf(h * acc[NK - 1], &sd, &cd);
         cs = c0 * cd - s0 * sd;
-        sn2 = s0 * cd + c0 * sd;
+        sn = s0 * cd + c0 * sd;
       }
-      rhs32<FULL>(R, F, tau, coef_tau_only, pn + dirf * (cfrac * h), y, cs, sn2, k[i]);
-    };
-    const float a2[6] = {(float)dp::A21, 0, 0, 0, 0, 0};
-    const float a3[6] = {(float)dp::A31, (float)dp::A32, 0, 0, 0, 0};
-    const float a4[6] = {(float)dp::A41, (float)dp::A42, (float)dp::A43, 0, 0, 0};
-    const float a5[6] = {(float)dp::A51, (float)dp::A52, (float)dp::A53, (float)dp::A54, 0, 0};
-    const float a6[6] = {(float)dp::A61, (float)dp::A62, (float)dp::A63, (float)dp::A64, (float)dp::A65, 0};
-    const float a7[6] = {(float)dp::B1, 0, (float)dp::B3, (float)dp::B4, (float)dp::B5, (float)dp::B6};
-    stage(1, (float)dp::C2, a2);
-    stage(2, (float)dp::C3, a3);
-    stage(3, (float)dp::C4, a4);
-    stage(4, (float)dp::C5, a5);
-    stage(5, 1.0f, a6);
-    stage(6, 1.0f, a7);
+      rhs32(R, F, tau, coef_full, pn + dirf * (c_C[s] * h), y, cs, sn, dk);
+#pragma unroll
+      for (int c = 0; c < NK; ++c) K(s, c) = dk[c];
+      if (s == 6) {
+#pragma unroll
+        for (int c = 0; c < NK; ++c) inc[c] = h * acc[c];
+      }
+    }
     L.evals += 6;
-    // 5th-order increments and the embedded error estimate
-    float inc[NK], err[NK];
+    // embedded error estimate and odeint's default error checker:
+    // max_i |err_i| / (atol + rtol (|x_i| + |dt| |x'_i|))
+    float err[NK];
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
-      inc[c] = h * ((float)dp::B1 * k[0][c] + (float)dp::B3 * k[2][c] + (float)dp::B4 * k[3][c] +
-                    (float)dp::B5 * k[4][c] + (float)dp::B6 * k[5][c]);
-      err[c] = h * ((float)dp::E1 * k[0][c] + (float)dp::E3 * k[2][c] + (float)dp::E4 * k[3][c] +
-                    (float)dp::E5 * k[4][c] + (float)dp::E6 * k[5][c] + (float)dp::E7 * k[6][c]);
+      float a = 0.f;
+#pragma unroll
+      for (int j = 0; j < 7; ++j) a = fmaf(c_E[j], K(j, c), a);
+      err[c] = h * a;
     }
-    // odeint default error checker: max_i |err_i| / (atol + rtol (|x_i| + |dt| |x'_i|))
     const float adt = fabsf(h);
     float e;
     if (tau) {
-      e = fabsf(err[0]) / fmaf(rtol, fmaf(adt, fabsf(k[0][0]), fabsf((float)L.tau_seg)), atol);
+      e = fabsf(err[0]) / fmaf(rtol, fmaf(adt, fabsf(L.k1[0]), fabsf((float)L.tau_seg)), atol);
     } else {
       e = 0.f;
 #pragma unroll
-      for (int c = 0; c < (FULL ? 4 : 1); ++c) {
-        float r = fabsf(err[c]) / fmaf(rtol, fmaf(adt, fabsf(k[0][c]), fabsf(L.x[c])), atol);
+      for (int c = 0; c < NX; ++c) {
+        float r = fabsf(err[c]) / fmaf(rtol, fmaf(adt, fabsf(L.k1[c]), fabsf(L.x[c])), atol);
         e = fmaxf(e, r);
       }
       if (FULL) {
@@ -323,33 +385,19 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       L.dt *= (double)(0.9f * __powf(ee, -0.2f));
       if (max_dt != 0.0 && fabs(L.dt) > max_dt) L.dt = max_dt;
     }
-#pragma unroll
-    for (int c = 0; c < NK; ++c) L.k1[c] = k[6][c];
     if (tau) {
       const double tau_old = L.tau_seg;
       L.tau_seg = tau_old + (double)inc[0];
       if (L.tau_seg >= R.P.tau_max) {
-        // bisection on the dense output of this step (src/Observation.cpp:166-190)
         L.status |= JSH_ST_TAU_CROSSED;
-        const float ydiff = inc[0];
-        const float bspl = h * k[0][0] - ydiff;
-        const float r4 = ydiff - h * k[6][0] - bspl;
-        const float r5 = h * ((float)dp::D1 * k[0][0] + (float)dp::D3 * k[2][0] + (float)dp::D4 * k[3][0] +
-                              (float)dp::D5 * k[4][0] + (float)dp::D6 * k[5][0] + (float)dp::D7 * k[6][0]);
-        double t0 = t_old, t1 = t_new, xm = L.tau_seg, tm;
-        int it = 0;
-        while (fabs(xm - R.P.tau_max) > R.P.tau_precision) {
-          if (++it > 200) {
-            L.status |= JSH_ST_BISECT_LIMIT;
-            break;
-          }
-          tm = 0.5 * (t0 + t1);
-          float th = (float)((tm - t_old) / dt_used), th1 = 1.f - th;
-          xm = tau_old + (double)(th * (ydiff + th1 * (bspl + th * (r4 + th1 * r5))));
-          if (xm > R.P.tau_max) t1 = tm;
-          else t0 = tm;
+        double tc = crossing_time(tau_old, t_old, dt_used, h, K(0, 0), K(2, 0), K(3, 0), K(4, 0), K(5, 0),
+                                  K(6, 0), inc[0], R.P.tau_max, R.P.tau_precision);
+        if (tc < 0.0) {
+          // the reference keeps bisecting; stop at the last bracket's midpoint
+          L.status |= JSH_ST_BISECT_LIMIT;
+          tc = t_old + 0.5 * dt_used;
         }
-        L.t_cross = 0.5 * (t0 + t1);
+        L.t_cross = tc;
         L.trunc = true;
         L.nseg = L.seg + 1;
         L.tau_bg += L.tau_seg;
@@ -358,9 +406,11 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       }
     } else {
 #pragma unroll
-      for (int c = 0; c < (FULL ? 4 : 1); ++c) L.x[c] += inc[c];
+      for (int c = 0; c < NX; ++c) L.x[c] += inc[c];
       if (FULL) L.chi += (double)inc[NK - 1];
     }
+#pragma unroll
+    for (int c = 0; c < NK; ++c) L.k1[c] = K(6, c);
     return;
   }
 
@@ -410,12 +460,14 @@ template <bool FULL>
 __global__ void __launch_bounds__(128) transfer_static_mixed_kernel(const JshRequest* __restrict__ reqs,
                                                                      int n_req) {
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
+  extern __shared__ float ksh[];
   batch_prefix(reqs, n_req, base);
   unsigned long long w = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= base[n_req]) return;
+  const Stages<FULL ? 5 : 1> K{ksh};
   Lane L;
   lane_start(L, reqs, base, n_req, w);
-  while (L.phase != PH_IDLE) lane_step<FULL>(L, reqs, L.phase == PH_TAU);
+  while (L.phase != PH_IDLE) lane_step<FULL>(L, reqs, L.phase == PH_TAU, K);
 }
 
 // Persistent CTAs: each warp keeps 32 lanes busy, refilling idle lanes from
@@ -425,7 +477,9 @@ __global__ void __launch_bounds__(256) transfer_persistent_mixed_kernel(const Js
                                                                          int n_req, unsigned long long* queue,
                                                                          int refill) {
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
+  extern __shared__ float ksh[];
   batch_prefix(reqs, n_req, base);
+  const Stages<FULL ? 5 : 1> K{ksh};
   const unsigned long long total = base[n_req];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -451,12 +505,16 @@ __global__ void __launch_bounds__(256) transfer_persistent_mixed_kernel(const Js
       continue;
     }
     bool warp_tau = __all_sync(0xffffffffu, L.phase != PH_IQUV);
-    if (L.phase != PH_IDLE) lane_step<FULL>(L, reqs, warp_tau);
+    if (L.phase != PH_IDLE) lane_step<FULL>(L, reqs, warp_tau, K);
   }
 }
 
-}  // namespace
+template <bool FULL>
+constexpr size_t stage_smem(int block) {
+  return sizeof(float) * 7 * (FULL ? 5 : 1) * (size_t)block;
+}
 
+}  // namespace
 
 }  // namespace jsh
 
@@ -468,8 +526,10 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
   if (schedule == JSH_SCHED_STATIC) {
     const int bs = 128;
     unsigned blocks = (unsigned)((max_items + bs - 1) / bs);
-    if (full) transfer_static_mixed_kernel<true><<<blocks, bs, 0, stream>>>(d_reqs, n_req);
-    else transfer_static_mixed_kernel<false><<<blocks, bs, 0, stream>>>(d_reqs, n_req);
+    if (full)
+      transfer_static_mixed_kernel<true><<<blocks, bs, stage_smem<true>(bs), stream>>>(d_reqs, n_req);
+    else
+      transfer_static_mixed_kernel<false><<<blocks, bs, stage_smem<false>(bs), stream>>>(d_reqs, n_req);
     return cudaGetLastError();
   }
   int bs = shape.block_size;
@@ -481,8 +541,12 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
   if ((uint64_t)blocks * bs > need) blocks = (unsigned)((need + bs - 1) / bs);
   if (blocks == 0) blocks = 1;
   unsigned long long* q = (unsigned long long*)queue;
-  if (full) transfer_persistent_mixed_kernel<true><<<blocks, bs, 0, stream>>>(d_reqs, n_req, q, shape.refill_threshold);
-  else transfer_persistent_mixed_kernel<false><<<blocks, bs, 0, stream>>>(d_reqs, n_req, q, shape.refill_threshold);
+  if (full)
+    transfer_persistent_mixed_kernel<true><<<blocks, bs, stage_smem<true>(bs), stream>>>(d_reqs, n_req, q,
+                                                                                       shape.refill_threshold);
+  else
+    transfer_persistent_mixed_kernel<false><<<blocks, bs, stage_smem<false>(bs), stream>>>(d_reqs, n_req, q,
+                                                                                         shape.refill_threshold);
   return cudaGetLastError();
 }
 
@@ -491,8 +555,12 @@ int jsh_queue64_occupancy(int block_size);
 int jsh_persistent_occupancy(int precision, bool full, int block_size) {
   int n = 0;
   if (precision == JSH_PREC_MIXED) {
-    if (full) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<true>, block_size, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<false>, block_size, 0);
+    if (full)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<true>, block_size,
+                                                    stage_smem<true>(block_size));
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<false>, block_size,
+                                                    stage_smem<false>(block_size));
   } else {
     n = jsh_queue64_occupancy(block_size);
   }
