@@ -74,6 +74,7 @@ struct Lane {
   double chi;
   float x[4];
   float k1[5];
+  float s1;  // noise scale of k1
   int32_t nsteps, fails;
   uint32_t status;
   uint32_t evals, acc, rej;
@@ -216,20 +217,23 @@ __device__ __noinline__ double crossing_time(double tau_old, double t_old, doubl
 }
 
 // Coefficients (one call site per kernel); `full` = false stops after
-// k_I, eta_I (the tau pass, or I-only output).
-__device__ __forceinline__ void rhs32(const JshRequest& R, const JshFreqConst& F, bool tau, bool full, F3 p,
-                                      const float* y, float cs, float sn, float* dk) {
+// k_I, eta_I (the tau pass, or I-only output).  Returns the magnitude of
+// the terms summed into the derivatives (eta_I + k_I |I| for the Stokes
+// vector, k_I for tau): the scale of their FP32 rounding noise.
+__device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& F, bool tau, bool full, F3 p,
+                                       const float* y, float cs, float sn, float* dk) {
   Coef32 c;
   coef32_rt(R, F, p, full, c);
   if (tau) {
     dk[0] = c.kI;
     dk[1] = dk[2] = dk[3] = dk[4] = 0.f;
-    return;
+    return fabsf(c.kI);
   }
+  const float scale = fabsf(c.eI) + fabsf(c.kI * y[0]);
   if (!full) {
     dk[0] = c.eI - c.kI * y[0];
     dk[1] = dk[2] = dk[3] = dk[4] = 0.f;
-    return;
+    return scale;
   }
   float Qlab = cs * y[1] - sn * y[2];
   float Ulab = sn * y[1] + cs * y[2];
@@ -240,7 +244,11 @@ __device__ __forceinline__ void rhs32(const JshRequest& R, const JshFreqConst& F
   dk[2] = -c.kI * y[2] - sn * sQ + cs * sU;
   dk[3] = c.eV - c.kI * y[3] - c.kV * y[0] + c.kC * Ulab;
   dk[4] = c.kF;
+  return scale;
 }
+
+// FP32 unit roundoff; the error norm's noise floor is kNoise * h * scale.
+constexpr float kNoise = 4.0f * 5.9604645e-8f;
 
 // One Dormand-Prince attempt (or a phase transition) of an active lane.
 // warp_tau: every active lane of the warp is in its tau pass, so only k_I
@@ -254,8 +262,8 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
   const JshFreqConst F = R.mix.fc[L.f];
   const bool tau = (L.phase == PH_TAU);
   const bool coef_full = FULL && !(tau && warp_tau);
-  const double sgn = tau ? 1.0 : -1.0;
-  const double ddx = sgn * R.plane.dx, ddy = sgn * R.plane.dy, ddz = sgn * R.plane.dz;
+  const double ddx = tau ? R.plane.dx : -R.plane.dx, ddy = tau ? R.plane.dy : -R.plane.dy,
+               ddz = tau ? R.plane.dz : -R.plane.dz;
   const F3 dirf = f3((float)ddx, (float)ddy, (float)ddz);
   const double max_dt = tau ? R.mix.dt_max_pc : 0.0;
   // error-norm tolerances in FP32 (the norm needs a few digits; t and dt stay FP64)
@@ -291,7 +299,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     const float h = (float)L.dt;
     float dk[5];
     if (!L.init) {
-      rhs32(R, F, tau, coef_full, pn, L.x, c0, s0, dk);
+      L.s1 = rhs32(R, F, tau, coef_full, pn, L.x, c0, s0, dk);
 #pragma unroll
       for (int c = 0; c < NK; ++c) L.k1[c] = dk[c];
       L.evals++;
@@ -300,6 +308,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
 #pragma unroll
     for (int c = 0; c < NK; ++c) K(0, c) = L.k1[c];
     float inc[NK];
+    float smax = L.s1, s7 = 0.f;
 #pragma unroll 1
     for (int s = 1; s < 7; ++s) {
       float acc[NK];
@@ -320,7 +329,9 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
         cs = c0 * cd - s0 * sd;
         sn = s0 * cd + c0 * sd;
       }
-      rhs32(R, F, tau, coef_full, pn + dirf * (c_C[s] * h), y, cs, sn, dk);
+      const float sc = rhs32(R, F, tau, coef_full, pn + dirf * (c_C[s] * h), y, cs, sn, dk);
+      smax = fmaxf(smax, sc);
+      s7 = sc;
 #pragma unroll
       for (int c = 0; c < NK; ++c) K(s, c) = dk[c];
       if (s == 6) {
@@ -339,15 +350,19 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       for (int j = 0; j < 7; ++j) a = fmaf(c_E[j], K(j, c), a);
       err[c] = h * a;
     }
+    // FP32 resolution floor: an error estimate below the rounding noise of
+    // the terms it is computed from carries no information, so the
+    // tolerance never drops below kNoise * h * (their magnitude)
     const float adt = fabsf(h);
+    const float floor_ = kNoise * adt * smax;
     float e;
     if (tau) {
-      e = fabsf(err[0]) / fmaf(rtol, fmaf(adt, fabsf(L.k1[0]), fabsf((float)L.tau_seg)), atol);
+      e = fabsf(err[0]) / (fmaf(rtol, fmaf(adt, fabsf(L.k1[0]), fabsf((float)L.tau_seg)), atol) + floor_);
     } else {
       e = 0.f;
 #pragma unroll
       for (int c = 0; c < NX; ++c) {
-        float r = fabsf(err[c]) / fmaf(rtol, fmaf(adt, fabsf(L.k1[c]), fabsf(L.x[c])), atol);
+        float r = fabsf(err[c]) / (fmaf(rtol, fmaf(adt, fabsf(L.k1[c]), fabsf(L.x[c])), atol) + floor_);
         e = fmaxf(e, r);
       }
       if (FULL) {
@@ -411,6 +426,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     }
 #pragma unroll
     for (int c = 0; c < NK; ++c) L.k1[c] = K(6, c);
+    L.s1 = s7;
     return;
   }
 
