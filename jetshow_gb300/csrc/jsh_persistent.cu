@@ -247,8 +247,11 @@ __device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& 
   return scale;
 }
 
-// FP32 unit roundoff; the error norm's noise floor is kNoise * h * scale.
-constexpr float kNoise = 4.0f * 5.9604645e-8f;
+// FP32 unit roundoff; the Stokes error norm's noise floor is
+// kNoise * h * scale.  The rounding noise of the embedded error estimate of
+// a Stokes component is about 0.3 u h scale (four terms of magnitude
+// <= scale per derivative, weighted by |e_j| <= 0.05).
+constexpr float kNoise = 5.9604645e-8f;
 
 // One Dormand-Prince attempt (or a phase transition) of an active lane.
 // warp_tau: every active lane of the warp is in its tau pass, so only k_I
@@ -357,7 +360,8 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     const float floor_ = kNoise * adt * smax;
     float e;
     if (tau) {
-      e = fabsf(err[0]) / (fmaf(rtol, fmaf(adt, fabsf(L.k1[0]), fabsf((float)L.tau_seg)), atol) + floor_);
+      // no cancellation in dtau/dt = k_I: the plain odeint norm
+      e = fabsf(err[0]) / fmaf(rtol, fmaf(adt, fabsf(L.k1[0]), fabsf((float)L.tau_seg)), atol);
     } else {
       e = 0.f;
 #pragma unroll
@@ -366,8 +370,11 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
         e = fmaxf(e, r);
       }
       if (FULL) {
+        // a rotation error d chi moves (Q, U) by P d chi; the lab-frame norm
+        // of the reference would compare that with rtol (P + h |dQ/dt|),
+        // and |dQ/dt| ~ k_F P there
         float P = sqrtf(fmaf(L.x[1], L.x[1], L.x[2] * L.x[2]));
-        e = fmaxf(e, fabsf(err[NK - 1]) * P / fmaf(rtol, P, atol));
+        e = fmaxf(e, fabsf(err[NK - 1]) * P / (fmaf(rtol * P, fmaf(adt, fabsf(L.k1[NK - 1]), 1.f), atol) + floor_));
       }
     }
     if (!(e == e) || isinf(e)) {
