@@ -256,6 +256,27 @@ int jsh_observation_run_device(jsh_ctx* ctx, const jsh_model_desc* model,
  * context (synchronises the context's work first). */
 int jsh_last_stats(jsh_ctx* ctx, jsh_stats* stats);
 
+/* Allocation-free form of jsh_observation_run_device, for callers that must
+ * not allocate device memory: code running while a stream is captured
+ * (cudaMalloc is illegal there), hosts whose framework owns the device
+ * memory pool, loops that cannot take cudaMalloc's implicit device
+ * synchronisation.  No context: it renders on the current device, enqueued
+ * on `cuda_stream`, into the caller's DEVICE output planes, and calls no
+ * cudaMalloc, cudaFree or other allocating routine.  Its scratch is one
+ * 8 MiB file-scope device array that every GPU loading the library holds
+ * until exit; it limits a call to JSH_NOALLOC_MAX_PIXELS pixels,
+ * JSH_NOALLOC_MAX_ALONG columns, JSH_NOALLOC_MAX_NU frequencies and analytic
+ * (non-gridded) fields, and rejects larger requests with JSH_ERR_INVALID.
+ * Calls share the array: calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture.  No counterpart in the reference, which renders on the CPU. */
+#define JSH_NOALLOC_MAX_PIXELS 65536
+#define JSH_NOALLOC_MAX_ALONG 4096
+#define JSH_NOALLOC_MAX_NU 64
+int jsh_observation_run_noalloc(const jsh_model_desc* model, const jsh_plane_desc* plane, const double* nu_hz,
+                                int32_t n_nu, const jsh_params* params, void* cuda_stream,
+                                jsh_image* device_out);
+
 /* Ray generation on the device (ImagePlane + Image + Ray ctors): origins
  * [n_across*n_along][3], the common unit direction [3], pixel sizes
  * [n_across*n_along] (cm), all host buffers (any may be NULL). */
