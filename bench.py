@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=int, default=1, help="shrink the image (debug only)")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=64,
+                    help="requests of the replayed serving stream (0 skips the serving leg)")
     return ap.parse_args()
 
 
@@ -204,6 +206,34 @@ def errors_vs_converged(jet, plane, nu, outs, n_pix=2048):
     return res
 
 
+def serving_leg(ctx, n_requests):
+    """Replay the seeded Poisson request stream (200 requests/s, priors of
+    the model-fitting sweep) through the serving loop in real time; latency
+    is arrival to result on the host."""
+    from jetshow_gb300 import serving as S
+    stream = S.request_stream(n_requests, rate_hz=200.0, seed=42)
+    with S.Server(ctx, max_inflight_batches=3, max_batch_requests=16) as srv:
+        # one short stream first: pages in the result path and the host threads
+        S.run_stream(srv, [r for r in S.request_stream(8, rate_hz=200.0, seed=7) if r.size_label == "64x64"])
+        records, wall = S.run_stream(srv, stream)
+    lat = np.array([r["latency_ms"] for r in records])
+    queue = np.array([r["queue_ms"] for r in records])
+    items = sum(r["n_items"] for r in records)
+    by_size = {}
+    for label in S.SIZES:
+        sel = np.array([r["size"] == label for r in records])
+        if sel.any():
+            by_size[label] = {"n": int(sel.sum()), "p50_ms": float(np.percentile(lat[sel], 50)),
+                              "p99_ms": float(np.percentile(lat[sel], 99))}
+    return {"requests": len(records), "arrival_rate_hz": 200.0, "wall_s": wall,
+            "rays_per_s": items / wall, "work_items": int(items),
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "queue_p50_ms": float(np.percentile(queue, 50)), "queue_p99_ms": float(np.percentile(queue, 99)),
+            "by_size": by_size, "admission_rejections": 0,
+            "mean_batch_requests": float(np.mean([r["batch_size"] for r in records])),
+            "tolerances": "rtol 1e-6 / 1e-7 tau, atol 1e-24 / 1e-20 tau, mixed precision, full Stokes"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -320,6 +350,7 @@ def main():
                      "frac": evals_per_s * CENSUS_MUFU / 1e12 / peaks["mufu_tops"]},
             "fp64_peak_tflops": peaks["fp64_tflops"]}
     cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 else None
+    serving = serving_leg(ctx, args.serve_requests) if args.serve_requests > 0 else None
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -337,7 +368,7 @@ def main():
                 "err_vs_converged_oracle": rel,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": float(np.mean(e2e_ms))},
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
                 "gpu_launches": 4, "rhs_evals_per_step": st_b["rhs_evals"],
                 "steps_accepted": st_b["steps_accepted"], "steps_rejected": st_b["steps_rejected"]}
         print(json.dumps(line), flush=True)

@@ -191,8 +191,19 @@ typedef struct jsh_params {
   int32_t block_size;      /* 0 = autotuned / default                               */
   int32_t refill_threshold;/* persistent schedule: refill when this many lanes idle  */
   int32_t ctas_per_sm;     /* persistent schedule: 0 = occupancy maximum             */
-  int32_t reserved;
+  int32_t flags;           /* JSH_FLAG_* (0 = defaults)                              */
 } jsh_params;
+
+/* Mixed precision: start the IQUV pass of an optically thick ray where the
+ * optical depth from the observer first exceeds tau_thick = 30 / (1 - p)
+ * (p = k_Q / k_I + 0.05, at most 0.95; p = 0 for I-only output) instead of
+ * at tau_max.  The Stokes vector entering at that depth reaches the observer
+ * attenuated by at least exp(-30) ~ 1e-13, so the image agrees with the
+ * integration from tau_max to that factor; thick rays need a small fraction
+ * of the stiff IQUV steps.  This flag turns it off (integrate from tau_max
+ * like src/Observation.cpp:242-274).  The FP64 path always integrates from
+ * tau_max. */
+#define JSH_FLAG_IQUV_FROM_TAU_MAX 0x1
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,

@@ -29,6 +29,7 @@ ST_NAN = 0x20
 ST_UB_GEOMETRY = 0x40
 ST_DT_UNDERFLOW = 0x80
 ST_IQUV = 0x100
+FLAG_IQUV_FROM_TAU_MAX = 0x1
 ST_ERRORS = ST_STEP_LIMIT | ST_FAIL_LIMIT | ST_BISECT_LIMIT | ST_NAN | ST_DT_UNDERFLOW
 
 GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE = 1, 2, 3, 4
@@ -134,7 +135,7 @@ class Params(C.Structure):
         ("block_size", C.c_int32),
         ("refill_threshold", C.c_int32),
         ("ctas_per_sm", C.c_int32),
-        ("reserved", C.c_int32),
+        ("flags", C.c_int32),
     ]
 
 

@@ -21,7 +21,7 @@ REPO = os.path.dirname(HERE)
 LIB = os.path.join(OUT, "libjetshow_gb300.so")
 
 CU_SOURCES = ["jsh_kernels.cu", "jsh_fp64.cu", "jsh_persistent.cu", "jsh_noalloc.cu"]
-CPP_SOURCES = ["jsh_host.cpp", "jsh_capi.cpp", "jsh_pending.cpp"]
+CPP_SOURCES = ["jsh_host.cpp", "jsh_capi.cpp", "jsh_server.cpp", "jsh_autotune.cpp", "jsh_grid.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -82,9 +82,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if force or not _newer(LIB, objs):
         _run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", LIB,
               "-lcudart_static", "-ldl", "-lrt", "-lpthread"])
-    with open(os.path.join(OUT, "ptxas.log"), "a") as fh:
-        for o, txt in logs.items():
-            fh.write(f"== {os.path.basename(o)}\n{txt}\n")
+    for o, txt in logs.items():  # one resource report per recompiled object
+        with open(o + ".ptxas.log", "w") as fh:
+            fh.write(txt)
     if verbose:
         for o, txt in logs.items():
             print(f"== {os.path.basename(o)}\n{txt}", file=sys.stderr)

@@ -180,6 +180,7 @@ int jsh_prepare_request(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_pla
   D.full = (P.output == JSH_OUT_FULL);
   D.precision = P.precision;
   D.schedule = P.schedule;
+  D.flags = P.flags;
   D.tau_max = P.tau_max;
   D.tau_min = P.tau_min;
   D.dt_max = P.dt_max;
@@ -258,7 +259,7 @@ extern "C" void jsh_ctx_destroy(jsh_ctx* c) {
   delete c;
 }
 
-namespace {
+// context-workspace helpers, shared with the autotuner (jsh_autotune.cpp)
 
 int ensure_workspace(jsh_ctx* ctx, size_t need) {
   if (need <= ctx->ws_cap) return JSH_OK;
@@ -362,7 +363,7 @@ int collect_stats(jsh_ctx* ctx, jsh_stats* s) {
   return JSH_OK;
 }
 
-}  // namespace
+
 
 extern "C" int jsh_observation_run(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_desc* plane,
                                    const double* nu_hz, int32_t n_nu, const jsh_params* params, jsh_image* host_out,

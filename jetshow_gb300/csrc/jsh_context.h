@@ -69,4 +69,13 @@ int jsh_alloc_device(jsh_ctx* ctx, size_t bytes, void** p);
 int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc_host);
 void jsh_free_device(jsh_ctx* ctx, void* p, size_t bytes);
 JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params);
+// Grow the context workspace to `need` bytes (waits for its previous user).
+int ensure_workspace(jsh_ctx* ctx, size_t need);
+// Enqueue one request on `stream` in the context workspace; dev_out NULL
+// keeps the outputs in workspace-owned planes.  Called with ctx->mu held.
+int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_desc* plane, const double* nu_hz,
+                   int32_t n_nu, const jsh_params* params, cudaStream_t stream, const jsh_image* dev_out,
+                   JshRequestLayout* L_out, uint64_t* npix_out);
+// Counters of the last enqueued request (synchronises with it).
+int collect_stats(jsh_ctx* ctx, jsh_stats* s);
 void jsh_set_error(const char* fmt, ...);

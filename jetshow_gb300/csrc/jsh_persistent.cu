@@ -29,6 +29,8 @@
 #include <float.h>
 #include <math.h>
 
+#include <algorithm>
+
 #include "jsh_batch.cuh"
 #include "jsh_context.h"
 #include "jsh_fields.cuh"
@@ -64,13 +66,14 @@ struct Lane {
   uint32_t h;
   uint8_t phase;
   int8_t seg, nseg;
-  bool init, trunc;
+  int8_t first_seg;      // segment where the IQUV pass starts inside (-1: at its end)
+  bool init;
   double p0x, p0y, p0z;  // segment start [pc]
   double length;         // [pc]
   double length_cm;
   double t, dt;          // [pc]
   double tau_seg, tau_bg, thick;
-  double t_cross;        // [pc] tau_max point on the last tau segment
+  double t_first;        // [pc] IQUV start on first_seg: tau_max crossing or optically thick point
   double chi;
   float x[4];
   float k1[5];
@@ -119,8 +122,9 @@ __device__ __forceinline__ void begin_tau_segment(Lane& L, const JshRequest& R, 
 __device__ __forceinline__ void begin_iquv_segment(Lane& L, const JshRequest& R, const JshHit& H) {
   int s = L.seg;
   double ox = H.seg[s][3], oy = H.seg[s][4], oz = H.seg[s][5];
-  if (L.trunc && s == L.nseg - 1) {
-    double tc = L.t_cross * JSH_PC;
+  if (s == L.first_seg) {
+    L.first_seg = -1;
+    double tc = L.t_first * JSH_PC;
     ox = H.seg[s][0] + R.plane.rx * tc;
     oy = H.seg[s][1] + R.plane.ry * tc;
     oz = H.seg[s][2] + R.plane.rz * tc;
@@ -150,10 +154,10 @@ __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict
   L.phase = PH_TAU;
   L.seg = 0;
   L.nseg = (int8_t)H.nseg;
-  L.trunc = false;
+  L.first_seg = -1;
   L.tau_bg = 0.0;
   L.thick = 0.0;
-  L.t_cross = -1.0;
+  L.t_first = -1.0;
   L.chi = 0.0;
   L.x[0] = L.x[1] = L.x[2] = L.x[3] = 0.f;
   L.status = (uint32_t)H.status | JSH_ST_HIT;
@@ -410,6 +414,12 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     if (tau) {
       const double tau_old = L.tau_seg;
       L.tau_seg = tau_old + (double)inc[0];
+      if (L.first_seg < 0 && L.tau_bg + L.tau_seg >= R.mix.tau_thick) {
+        // optically thick from here on: the IQUV pass starts at the end of
+        // this step (the tau pass goes on for the tau image)
+        L.first_seg = L.seg;
+        L.t_first = t_new;
+      }
       if (L.tau_seg >= R.P.tau_max) {
         L.status |= JSH_ST_TAU_CROSSED;
         double tc = crossing_time(tau_old, t_old, dt_used, h, K(0, 0), K(2, 0), K(3, 0), K(4, 0), K(5, 0),
@@ -419,8 +429,10 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
           L.status |= JSH_ST_BISECT_LIMIT;
           tc = t_old + 0.5 * dt_used;
         }
-        L.t_cross = tc;
-        L.trunc = true;
+        if (L.first_seg < 0 || (L.first_seg == L.seg && tc < L.t_first)) {
+          L.first_seg = L.seg;
+          L.t_first = tc;
+        }
         L.nseg = L.seg + 1;
         L.tau_bg += L.tau_seg;
         L.thick += L.length_cm;
@@ -465,7 +477,7 @@ start_iquv : {
   }
   L.status |= JSH_ST_IQUV;
   L.phase = PH_IQUV;
-  L.seg = L.nseg - 1;
+  L.seg = L.first_seg >= 0 ? L.first_seg : L.nseg - 1;
   begin_iquv_segment(L, R, R.hits[L.h]);
   return;
 }
@@ -608,6 +620,15 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   X.dt_max_pc = req->P.dt_max / JSH_PC;
   X.kq = (float)m.kq_ratio;
   X.eq = (float)m.eq_ratio;
+  // optically thick start of the IQUV pass: the Stokes vector decays at
+  // least at rate k_I (1 - |(k_Q, k_U, k_V)| / k_I) along the ray (the
+  // symmetric part of the transfer matrix; Faraday terms only rotate), so
+  // what enters at optical depth tau_thick is attenuated by exp(-30)
+  {
+    double p = req->P.full ? std::min(0.95, m.kq_ratio + 0.05) : 0.0;
+    double thick = 30.0 / (1.0 - p);
+    X.tau_thick = (req->P.flags & JSH_FLAG_IQUV_FROM_TAU_MAX) || !(thick < req->P.tau_max) ? INFINITY : thick;
+  }
   if (m.v_kind == JSH_V_CONST_FLAT) {
     // getG, getD, get_n_los_prime (src/utils.cpp:147-162) in FP64
     double g = m.vp[0];

@@ -15,7 +15,7 @@ struct JshHit {           // one intersecting pixel (Intersection list)
 };
 
 struct JshParamsDev {
-  int32_t n, full, precision, schedule;
+  int32_t n, full, precision, schedule, flags, pad_;
   double tau_max, tau_min, dt_max;
   double tau_atol, tau_rtol, atol, rtol, tau_precision;
   int64_t max_steps;
@@ -38,8 +38,9 @@ struct JshMixed {
   float nl[3];           // LOS towards the observer (-ray direction)
   float pk;              // (s + 2) / 2
   float kq, eq;          // k_Q / k_I, eta_Q / eta_I
-  float reserved;
+  float pad_;
   double dt_max_pc;      // tau-pass step limit [pc], 0 = none
+  double tau_thick;      // IQUV pass starts where the optical depth first exceeds this
   const JshFreqConst* fc;  // device [n_nu]
 };
 

@@ -404,7 +404,7 @@ class Observation:
 
 def make_params(n=100, tau_max=1e4, dt_max=0.0, tau_min=1e-10, output="I", precision="fp64",
                 schedule="static", tau_atol=1E-7, tau_rtol=1E-14, atol=1E-9, rtol=1E-9, tau_precision=1.0,
-                max_steps=0, block_size=0, refill_threshold=0, ctas_per_sm=0) -> A.Params:
+                max_steps=0, block_size=0, refill_threshold=0, ctas_per_sm=0, flags=0) -> A.Params:
     out = {"I": A.OUT_I, "full": A.OUT_FULL}[output] if isinstance(output, str) else int(output)
     prec = {"fp64": A.PREC_FP64, "mixed": A.PREC_MIXED}[precision] if isinstance(precision, str) else int(precision)
     sch = ({"static": A.SCHED_STATIC, "persistent": A.SCHED_PERSISTENT}[schedule]
@@ -414,4 +414,4 @@ def make_params(n=100, tau_max=1e4, dt_max=0.0, tau_min=1e-10, output="I", preci
                     tau_rtol=float(tau_rtol), atol=float(atol), rtol=float(rtol),
                     tau_precision=float(tau_precision), max_steps=int(max_steps),
                     block_size=int(block_size), refill_threshold=int(refill_threshold),
-                    ctas_per_sm=int(ctas_per_sm))
+                    ctas_per_sm=int(ctas_per_sm), flags=int(flags))

@@ -69,6 +69,16 @@ class Context:
                                                             A.dptr(nu), nu.size, C.byref(params),
                                                             C.c_void_p(stream_ptr), C.byref(img)))
 
+    def autotune(self, model: A.ModelDesc, plane: A.PlaneDesc, nu, params: A.Params) -> dict:
+        """Search the persistent schedule's launch shape on this request and
+        make the fastest the context default (results do not depend on it)."""
+        nu = np.ascontiguousarray(np.atleast_1d(nu), dtype=np.float64)
+        t = A.Tuning()
+        check(self.lib, self.lib.jsh_autotune(self.handle, C.byref(model), C.byref(plane), A.dptr(nu), nu.size,
+                                              C.byref(params), C.byref(t)))
+        return {"block_size": t.block_size, "ctas_per_sm": t.ctas_per_sm, "refill_threshold": t.refill_threshold,
+                "ms": t.ms}
+
     def last_stats(self):
         st = A.Stats()
         check(self.lib, self.lib.jsh_last_stats(self.handle, C.byref(st)))
@@ -104,6 +114,42 @@ class Context:
                                               n, nseg.ctypes.data_as(C.POINTER(C.c_int32)), A.dptr(seg),
                                               st.ctypes.data_as(C.POINTER(C.c_uint32))))
         return nseg, seg, st
+
+    # ---------------------------------------------------------- gridded fields
+    def grid_upload(self, xy, values, tri) -> int:
+        """Upload a triangulated (z, r) grid [pc] with per-vertex FP32
+        values [n, n_fields]; returns the grid id for Simulation*Field."""
+        xy = np.ascontiguousarray(xy, dtype=np.float64)
+        values = np.ascontiguousarray(values, dtype=np.float32)
+        if values.ndim == 1:
+            values = values[:, None]
+        tri = np.ascontiguousarray(tri, dtype=np.int32)
+        gid = C.c_int32()
+        check(self.lib, self.lib.jsh_grid_upload(self.handle, A.dptr(xy), xy.shape[0],
+                                                 values.ctypes.data_as(C.POINTER(C.c_float)), values.shape[1],
+                                                 tri.ctypes.data_as(C.POINTER(C.c_int32)), tri.shape[0],
+                                                 C.byref(gid)))
+        return gid.value
+
+    def grid_interpolate(self, grid_id: int, field: int, zr, nan_value=0.0):
+        """Values of field `field` at points (z, r) [pc], interpolated on the device."""
+        zr = np.ascontiguousarray(zr, dtype=np.float64).reshape(-1, 2)
+        out = np.empty(zr.shape[0])
+        check(self.lib, self.lib.jsh_grid_interpolate(self.handle, grid_id, field, A.dptr(zr), zr.shape[0],
+                                                      float(nan_value), A.dptr(out)))
+        return out
+
+
+def triangulate(xy) -> np.ndarray:
+    """Delaunay triangulation of points xy [n, 2] on the host
+    (jsh_grid_triangulate): int32 [n_tri, 3], counter-clockwise."""
+    lib = A.load_library()
+    xy = np.ascontiguousarray(xy, dtype=np.float64)
+    tri = np.empty((2 * xy.shape[0], 3), np.int32)
+    m = C.c_int64()
+    check(lib, lib.jsh_grid_triangulate(A.dptr(xy), xy.shape[0], tri.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        C.byref(m)))
+    return tri[:m.value].copy()
 
 
 def stats_dict(st: A.Stats) -> dict:

@@ -87,3 +87,104 @@ def parabolic_c2(scale=1, n_freq=2):
     plane = J.ImagePlane((n, n), _lg_cm(mas), _lg_cm(mas), 0.05)
     nu = np.array([5.0e9, 15.4e9][:n_freq]) * (1 + Z)
     return jet, plane, nu, dict(TRANSFER_KW)
+
+
+# ----------------------------------------------------------------- C3
+def scrambled_sobol2(n: int, seed: int = 0, bits: int = 30) -> np.ndarray:
+    """n points of the 2-D Sobol sequence (dimension 1: van der Corput;
+    dimension 2: primitive polynomial x + 1, m_1 = 1) with Matousek's
+    random linear scramble and a random digital shift, both drawn from
+    ``seed``.  Returns float64 [n, 2] in [0, 1)."""
+    rng = np.random.default_rng(seed)
+    idx = np.arange(n, dtype=np.uint64)
+    # direction numbers v_k = m_k 2^(bits - k), k = 1..bits
+    m = [1]
+    for _ in range(1, bits):
+        m.append((2 * m[-1]) ^ m[-1])
+    dirs = [[1 << (bits - k) for k in range(1, bits + 1)], [m[k - 1] << (bits - k) for k in range(1, bits + 1)]]
+    out = np.empty((n, 2))
+    for d in range(2):
+        x = np.zeros(n, dtype=np.uint64)
+        for k in range(bits):
+            x ^= ((idx >> np.uint64(k)) & np.uint64(1)) * np.uint64(dirs[d][k])
+        # linear scramble: output bit j (from the most significant) is the
+        # parity of input bits 0..j under a random lower-triangular matrix
+        # with unit diagonal; then a random digital shift
+        y = np.zeros(n, dtype=np.uint64)
+        for j in range(bits):
+            row = rng.integers(0, 2, size=j + 1)
+            row[j] = 1
+            mask = 0
+            for i in range(j + 1):
+                if row[i]:
+                    mask |= 1 << (bits - 1 - i)
+            p = x & np.uint64(mask)
+            for s in (32, 16, 8, 4, 2, 1):
+                p ^= p >> np.uint64(s)
+            y |= (p & np.uint64(1)) << np.uint64(bits - 1 - j)
+        y ^= np.uint64(int(rng.integers(0, 1 << bits)))
+        out[:, d] = y.astype(np.float64) / float(1 << bits)
+    return out
+
+
+def gaussian_random_field(z_max=20.0, r_max=0.5, step=0.0125, corr=0.05, seed=1):
+    """Unit-variance Gaussian random field on a lattice of `step` pc over
+    [0, z_max] x [0, r_max]: white noise (seeded) convolved with a Gaussian
+    kernel of width corr / sqrt(2), so that the field's correlation is
+    exp(-d^2 / (2 corr^2)).  Returns (lattice values [nz, nr], step)."""
+    rng = np.random.default_rng(seed)
+    sk = corr / math.sqrt(2.0) / step  # kernel width in lattice steps
+    half = int(math.ceil(4 * sk))
+    ker = np.exp(-0.5 * (np.arange(-half, half + 1) / sk) ** 2)
+    ker /= np.sqrt(np.sum(ker ** 2))
+    nz, nr = int(round(z_max / step)) + 1, int(round(r_max / step)) + 1
+    noise = rng.standard_normal((nz + 2 * half, nr + 2 * half))
+    g = np.apply_along_axis(lambda v: np.convolve(v, ker, mode="valid"), 0, noise)
+    g = np.apply_along_axis(lambda v: np.convolve(v, ker, mode="valid"), 1, g)
+    return g, step
+
+
+def bilinear(lattice, step, z, r):
+    fz, fr = z / step, r / step
+    i = np.clip(np.floor(fz).astype(int), 0, lattice.shape[0] - 2)
+    j = np.clip(np.floor(fr).astype(int), 0, lattice.shape[1] - 2)
+    tz, tr = fz - i, fr - j
+    return ((1 - tz) * (1 - tr) * lattice[i, j] + tz * (1 - tr) * lattice[i + 1, j] +
+            (1 - tz) * tr * lattice[i, j + 1] + tz * tr * lattice[i + 1, j + 1])
+
+
+C3_FIELDS = ("B_p", "B_phi", "n", "Gamma")
+
+
+def simulation_grid_c3(n_points=200_000, sigma=0.3):
+    """The C3 simulation grid: scrambled Sobol points (seed 0) over
+    z in [0, 20] pc, r in [0, 0.5] pc; values B_p, B_phi, n, Gamma of the
+    conical jet's laws (B = 0.1 G (R/pc)^-1 split equally poloidal /
+    toroidal, n = 500 (R/pc)^-2, Gamma = 10; R = sqrt(z^2 + r^2)) times
+    exp(sigma g) with g the seeded Gaussian random field (correlation
+    0.05 pc), FP32.  Returns (xy [n, 2] float64 (z, r) pc, values [n, 4]
+    float32)."""
+    u = scrambled_sobol2(n_points, seed=0)
+    z, r = 20.0 * u[:, 0], 0.5 * u[:, 1]
+    lat, step = gaussian_random_field()
+    f = np.exp(sigma * bilinear(lat, step, z, r))
+    R = np.hypot(z, r)
+    b = 0.1 * (1.0 / R) / math.sqrt(2.0)
+    vals = np.column_stack([b * f, b * f, 500.0 * R ** -2 * f, 10.0 * f]).astype(np.float32)
+    return np.column_stack([z, r]), vals
+
+
+def simulation_c3(grid_id: int, scale=1):
+    """C3 render on an uploaded C3 grid: Cone (half-angle 0.05) as the
+    envelope, every field from the grid (nan_value outside its hull:
+    B = n = 0, Gamma = 1), LOS 0.1 rad, 512x512 uniform pixels of 0.002 mas
+    (the grid's z <= 20 pc projects to 1.08 mas), 15.4 GHz."""
+    n = max(2, 512 // scale)
+    n += n % 2
+    mas = 0.002 * 512 / n
+    geo = J.Cone((0, 0, 0), (0, 0, 1), 0.05, 100.0 * J.pc)
+    jet = J.Jet(geo, J.SimulationVField(grid_id, 3), J.SimulationBField(grid_id, 0, 1, True),
+                J.SimulationNField(grid_id, 2, True), s=2.5, gamma_min=10.0)
+    plane = J.ImagePlane((n, n), _lg_cm(mas), _lg_cm(mas), 0.1)
+    nu = np.array([15.4e9]) * (1 + Z)
+    return jet, plane, nu, dict(TRANSFER_KW)

@@ -1188,6 +1188,10 @@ static void render_ray(const model_t* m, v3 ro, v3 rd, v3 rd_renorm, double nu, 
   for (int i = 0; i < 4; ++i) o->iquv[i] = st[i];
 }
 
+/* Optional per-item RHS evaluation counts of the next renders ([n_nu][n_sel]). */
+static uint64_t* g_item_evals = NULL;
+void jo_set_item_evals(uint64_t* buf) { g_item_evals = buf; }
+
 int jo_render(const jsh_model_desc* model, const jsh_plane_desc* plane, const double* nu, int32_t n_nu,
               const jsh_params* params, const int64_t* pix_idx, int64_t n_sel, int32_t n_threads, jsh_image* out,
               jo_counters* counters) {
@@ -1225,6 +1229,7 @@ int jo_render(const jsh_model_desc* model, const jsh_plane_desc* plane, const do
     if (out->U) out->U[q] = o.iquv[2];
     if (out->V) out->V[q] = o.iquv[3];
     if (out->status) out->status[q] = o.status;
+    if (g_item_evals) g_item_evals[q] = c.rhs_evals;
     tot_evals += c.rhs_evals;
     tot_acc += c.steps_accepted;
     tot_rej += c.steps_rejected;

@@ -47,6 +47,10 @@ int jo_render(const jsh_model_desc* model, const jsh_plane_desc* plane,
               const int64_t* pix_idx, int64_t n_sel, int32_t n_threads,
               jsh_image* out, jo_counters* counters);
 
+/* Per-item RHS evaluation counts of later jo_render calls are written to
+ * buf[n_nu][n_sel] when buf is not NULL (cost profiling of the workloads). */
+void jo_set_item_evals(uint64_t* buf);
+
 /* All eleven transfer coefficients at a lab-frame point for the LOS unit
  * vector n_los (pointing to the observer) and frequency nu:
  * out = {kI, kQ, kU, kV, kF, kC, hQ, etaI, etaQ, etaU, etaV}. */

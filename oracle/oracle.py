@@ -47,6 +47,8 @@ def lib():
         P, D = C.POINTER, C.POINTER(C.c_double)
         L.jo_plane_rays.argtypes = [P(A.PlaneDesc), D, D, D]
         L.jo_hit_rays.argtypes = [P(A.ModelDesc), D, D, C.c_int64, P(C.c_int32), D, P(C.c_uint32)]
+        L.jo_set_item_evals.argtypes = [P(C.c_uint64)]
+        L.jo_set_item_evals.restype = None
         L.jo_render.argtypes = [P(A.ModelDesc), P(A.PlaneDesc), D, C.c_int32, P(A.Params),
                                 P(C.c_int64), C.c_int64, C.c_int32, P(A.Image), P(Counters)]
         L.jo_coefficients.argtypes = [P(A.ModelDesc), D, D, C.c_double, D]
@@ -90,9 +92,10 @@ def hit_rays(model: A.ModelDesc, origins, directions):
     return nseg, seg, st
 
 
-def render(model: A.ModelDesc, plane: A.PlaneDesc, nu, params: A.Params, pix=None, threads=0):
+def render(model: A.ModelDesc, plane: A.PlaneDesc, nu, params: A.Params, pix=None, threads=0, item_evals=False):
     """Render (all pixels or the flat pixel indices ``pix``); returns a dict of
-    [n_nu, n_sel] arrays plus counters."""
+    [n_nu, n_sel] arrays plus counters (and the per-item RHS evaluation
+    counts as ``evals`` when ``item_evals``)."""
     nu = np.ascontiguousarray(np.atleast_1d(nu), dtype=np.float64)
     npix = int(plane.n_across * plane.n_along)
     if pix is None:
@@ -107,8 +110,15 @@ def render(model: A.ModelDesc, plane: A.PlaneDesc, nu, params: A.Params, pix=Non
     img = A.Image(*(A.dptr(out[k]) for k in ("tau", "l", "I", "Q", "U", "V")),
                   out["status"].ctypes.data_as(C.POINTER(C.c_uint32)))
     cnt = Counters()
-    _chk(lib().jo_render(C.byref(model), C.byref(plane), A.dptr(nu), nu.size, C.byref(params),
-                         pix_p, nsel, threads, C.byref(img), C.byref(cnt)))
+    if item_evals:
+        out["evals"] = np.zeros((nu.size, nsel), np.uint64)
+        lib().jo_set_item_evals(out["evals"].ctypes.data_as(C.POINTER(C.c_uint64)))
+    try:
+        _chk(lib().jo_render(C.byref(model), C.byref(plane), A.dptr(nu), nu.size, C.byref(params),
+                             pix_p, nsel, threads, C.byref(img), C.byref(cnt)))
+    finally:
+        if item_evals:
+            lib().jo_set_item_evals(None)
     out["rhs_evals"] = cnt.rhs_evals
     out["steps_accepted"] = cnt.steps_accepted
     out["steps_rejected"] = cnt.steps_rejected
