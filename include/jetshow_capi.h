@@ -204,6 +204,9 @@ typedef struct jsh_params {
  * like src/Observation.cpp:242-274).  The FP64 path always integrates from
  * tau_max. */
 #define JSH_FLAG_IQUV_FROM_TAU_MAX 0x1
+/* Cost map: the l plane receives each item's number of right-hand-side
+ * evaluations instead of the path length (schedule and cost studies). */
+#define JSH_FLAG_COST_MAP 0x2
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,

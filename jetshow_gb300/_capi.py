@@ -30,6 +30,7 @@ ST_UB_GEOMETRY = 0x40
 ST_DT_UNDERFLOW = 0x80
 ST_IQUV = 0x100
 FLAG_IQUV_FROM_TAU_MAX = 0x1
+FLAG_COST_MAP = 0x2
 ST_ERRORS = ST_STEP_LIMIT | ST_FAIL_LIMIT | ST_BISECT_LIMIT | ST_NAN | ST_DT_UNDERFLOW
 
 GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE = 1, 2, 3, 4

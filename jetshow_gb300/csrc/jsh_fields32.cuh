@@ -61,65 +61,66 @@ __device__ __forceinline__ F3 parabolic_dir(float Rz0_pc, F3 p) {
   return f3(ca * p.x / r, ca * p.y / r, sa);
 }
 
-__device__ inline Vel vfield32(const JshModel& m, F3 p) {
-  const double* q = m.vp;
+__device__ inline Vel vfield32(const JshModel& m, const JshMixed& X, F3 p) {
+  const float* q = X.vq;
+  const float* qp = X.vq_pc;
   const float inv_pc = (float)(1.0 / JSH_PC);
   switch (m.v_kind) {
-    case JSH_V_CONST_FLAT: return Vel{(float)q[0], f3(0, 0, 1)};
+    case JSH_V_CONST_FLAT: return Vel{q[0], f3(0, 0, 1)};
     case JSH_V_SHEARED_FLAT: {
       float r = sqrtf(p.x * p.x + p.y * p.y);
-      float g = (float)q[0] - (float)(q[0] - q[1]) * r / (float)(q[2] / JSH_PC);
+      float g = q[0] - X.v_dq01 * r / qp[2];
       return Vel{g, f3(0, 0, 1)};
     }
     case JSH_V_SHEATH_FLAT: {
       float r = sqrtf(p.x * p.x + p.y * p.y);
-      return Vel{r < (float)(q[2] / JSH_PC) ? (float)q[0] : (float)q[1], f3(0, 0, 1)};
+      return Vel{r < qp[2] ? q[0] : q[1], f3(0, 0, 1)};
     }
     case JSH_V_CONST_CENTRAL: {
-      F3 a = p + f3((float)q[1], (float)q[2], (float)q[3]) * inv_pc;
-      return Vel{(float)q[0], a * rsqrtf(fdot(a, a))};
+      F3 a = p + f3(q[1], q[2], q[3]) * inv_pc;
+      return Vel{q[0], a * rsqrtf(fdot(a, a))};
     }
     case JSH_V_SHEARED_CENTRAL: {
       // theta = acos(z + o_z / r) evaluated in cm as written (src/VField.cpp:83)
-      F3 a = p + f3((float)q[3], (float)q[4], (float)q[5]) * inv_pc;
+      F3 a = p + f3(q[3], q[4], q[5]) * inv_pc;
       float r_cm = sqrtf(fdot(a, a)) * (float)JSH_PC;
-      float theta = acosf(p.z * (float)JSH_PC + (float)q[5] / r_cm);
-      float g = (float)q[0] - (float)(q[0] - q[1]) * theta / (float)q[2];
+      float theta = acosf(p.z * (float)JSH_PC + q[5] / r_cm);
+      float g = q[0] - X.v_dq01 * theta / q[2];
       return Vel{g, a * rsqrtf(fdot(a, a))};
     }
     case JSH_V_SHEATH_CENTRAL: {
-      F3 a = p + f3((float)q[3], (float)q[4], (float)q[5]) * inv_pc;
+      F3 a = p + f3(q[3], q[4], q[5]) * inv_pc;
       float r = sqrtf(fdot(a, a));
       float theta = acosf(p.z / r);
-      return Vel{theta < (float)q[2] ? (float)q[0] : (float)q[1], a * (1.f / r)};
+      return Vel{theta < q[2] ? q[0] : q[1], a * (1.f / r)};
     }
-    case JSH_V_CONST_PARABOLIC: return Vel{(float)q[0], parabolic_dir((float)(q[1] / JSH_PC), p)};
+    case JSH_V_CONST_PARABOLIC: return Vel{q[0], parabolic_dir(qp[1], p)};
     case JSH_V_ACC_PARABOLIC: {
-      float g = 1.f + (float)(q[0] - 1.0) * sqrtf(p.z / (float)(q[1] / JSH_PC));
-      return Vel{g, parabolic_dir((float)(q[2] / JSH_PC), p)};
+      float g = 1.f + X.v_g0m1 * sqrtf(p.z / qp[1]);
+      return Vel{g, parabolic_dir(qp[2], p)};
     }
     case JSH_V_SHEARED_ACC_PARABOLIC:
     case JSH_V_SHEARED_ACC_PARABOLIC_CONST_CONE:
     case JSH_V_ACC_PARABOLIC_CONST_CONE: {
       int k = m.v_kind;
-      float z0_pc = (float)((k == JSH_V_ACC_PARABOLIC_CONST_CONE ? q[2] : q[3]) / JSH_PC);
+      float z0_pc = (k == JSH_V_ACC_PARABOLIC_CONST_CONE ? qp[2] : qp[3]);
       if (k != JSH_V_SHEARED_ACC_PARABOLIC && p.z > z0_pc) {
-        F3 a = p + f3(0.f, 0.f, (float)(m.v_cone_oz / JSH_PC));
+        F3 a = p + f3(0.f, 0.f, X.v_cone_oz_pc);
         F3 dir = a * rsqrtf(fdot(a, a));
-        if (k == JSH_V_ACC_PARABOLIC_CONST_CONE) return Vel{(float)q[0], dir};
+        if (k == JSH_V_ACC_PARABOLIC_CONST_CONE) return Vel{q[0], dir};
         float r_cm = sqrtf(fdot(a, a)) * (float)JSH_PC;
-        float theta = acosf(p.z * (float)JSH_PC + (float)m.v_cone_oz / r_cm);
-        return Vel{(float)q[0] - (float)(q[0] - q[1]) * theta / (float)m.v_theta, dir};
+        float theta = acosf(p.z * (float)JSH_PC + X.v_cone_oz / r_cm);
+        return Vel{q[0] - X.v_dq01 * theta / X.v_theta, dir};
       }
       if (k == JSH_V_ACC_PARABOLIC_CONST_CONE) {
-        float g = 1.f + (float)(q[0] - 1.0) * sqrtf(p.z / z0_pc);
-        return Vel{g, parabolic_dir((float)(q[1] / JSH_PC), p)};
+        float g = 1.f + X.v_g0m1 * sqrtf(p.z / z0_pc);
+        return Vel{g, parabolic_dir(qp[1], p)};
       }
-      float R0_pc = (k == JSH_V_SHEARED_ACC_PARABOLIC) ? (float)(q[2] / JSH_PC) : z0_pc;
-      float Rz0_pc = (float)((k == JSH_V_SHEARED_ACC_PARABOLIC ? q[3] : q[2]) / JSH_PC);
+      float R0_pc = (k == JSH_V_SHEARED_ACC_PARABOLIC) ? qp[2] : z0_pc;
+      float Rz0_pc = (k == JSH_V_SHEARED_ACC_PARABOLIC ? qp[3] : qp[2]);
       float r = hypotf(p.x, p.y);
       float R = sqrtf(Rz0_pc * Rz0_pc * p.z);
-      float g0 = (float)q[0] - (float)(q[0] - q[1]) * sqrtf(sqrtf(r / R));
+      float g0 = q[0] - X.v_dq01 * sqrtf(sqrtf(r / R));
       if (g0 < 1.f) g0 = 1.f;
       float g = 1.f + (g0 - 1.f) * sqrtf(p.z / R0_pc);
       return Vel{g, parabolic_dir(Rz0_pc, p)};
@@ -130,15 +131,16 @@ __device__ inline Vel vfield32(const JshModel& m, F3 p) {
 }
 
 // ---------------------------------------------------------------- N
-__device__ inline float nfield32(const JshModel& m, F3 p) {
-  const double* q = m.np;
+__device__ inline float nfield32(const JshModel& m, const JshMixed& X, F3 p) {
+  const float* q = X.nq;
+  const float* qp = X.nq_pc;
   switch (m.n_kind) {
-    case JSH_N_CONST: return (float)q[0];
-    case JSH_N_BK: return (float)q[0] * fpow(sqrtf(fdot(p, p)), -(float)q[1]);
-    case JSH_N_BKZ: return (float)q[0] * fpow(fabsf(p.z), -(float)q[1]);
+    case JSH_N_CONST: return q[0];
+    case JSH_N_BK: return q[0] * fpow(sqrtf(fdot(p, p)), -q[1]);
+    case JSH_N_BKZ: return q[0] * fpow(fabsf(p.z), -q[1]);
     case JSH_N_COMPOSITE_BK: {
-      float e = (fabsf(p.z) > (float)(q[3] / JSH_PC)) ? (float)q[2] : (float)q[1];
-      return (float)q[0] * fpow(sqrtf(fdot(p, p)), -e);
+      float e = (fabsf(p.z) > qp[3]) ? q[2] : q[1];
+      return q[0] * fpow(sqrtf(fdot(p, p)), -e);
     }
     case JSH_N_SIMULATION: return sim32(m.grids[1], m.f_n, p, 0.0f);
     default: return 0.f;
@@ -146,14 +148,15 @@ __device__ inline float nfield32(const JshModel& m, F3 p) {
 }
 
 // ---------------------------------------------------------------- B
-__device__ inline float bscalar32(const JshModel& m, F3 p) {
-  const double* q = m.bp;
+__device__ inline float bscalar32(const JshModel& m, const JshMixed& X, F3 p) {
+  const float* q = X.bq;
+  const float* qp = X.bq_pc;
   switch (m.b_kind) {
-    case JSH_B_RANDOM_SCALAR: return (float)q[0] * fpow(sqrtf(fdot(p, p)), -(float)q[1]);
-    case JSH_B_RANDOM_SCALAR_Z: return (float)q[0] * fpow(fabsf(p.z), -(float)q[1]);
+    case JSH_B_RANDOM_SCALAR: return q[0] * fpow(sqrtf(fdot(p, p)), -q[1]);
+    case JSH_B_RANDOM_SCALAR_Z: return q[0] * fpow(fabsf(p.z), -q[1]);
     case JSH_B_COMPOSITE_RANDOM_SCALAR_Z: {
-      float e = (fabsf(p.z) > (float)(q[3] / JSH_PC)) ? (float)q[2] : (float)q[1];
-      return (float)q[0] * fpow(fabsf(p.z), -e);
+      float e = (fabsf(p.z) > qp[3]) ? q[2] : q[1];
+      return q[0] * fpow(fabsf(p.z), -e);
     }
     default: return 0.f;
   }
@@ -170,52 +173,52 @@ __device__ __forceinline__ void sincos_atan(float u, float& s, float& c) {
   s = u * c;
 }
 
-__device__ inline F3 bvector32(const JshModel& m, F3 p) {
-  const double* q = m.bp;
+__device__ inline F3 bvector32(const JshModel& m, const JshMixed& X, F3 p) {
+  const float* q = X.bq;
   switch (m.b_kind) {
-    case JSH_B_CONST_CYLINDER: return f3(0, 0, (float)q[0] * fpow(sqrtf(fdot(p, p)), -(float)q[1]));
-    case JSH_B_CONST_CYLINDER_Z: return f3(0, 0, (float)q[0] * fpow(fabsf(p.z), -(float)q[1]));
+    case JSH_B_CONST_CYLINDER: return f3(0, 0, q[0] * fpow(sqrtf(fdot(p, p)), -q[1]));
+    case JSH_B_CONST_CYLINDER_Z: return f3(0, 0, q[0] * fpow(fabsf(p.z), -q[1]));
     case JSH_B_RADIAL_CONICAL: {
       float r = sqrtf(fdot(p, p));
-      return p * ((float)q[0] * fpow(r, -(float)q[1]) / r);
+      return p * (q[0] * fpow(r, -q[1]) / r);
     }
     case JSH_B_TOROIDAL: {
       float s, c;
       sincos_atan(p.y / p.x, s, c);
-      float b = (float)q[0] * fpow(p.z, -(float)q[1]);
+      float b = q[0] * fpow(p.z, -q[1]);
       return f3(-s * b, c * b, 0.f);
     }
     case JSH_B_HELICAL_CYLINDER: {
       float r = sqrtf(p.x * p.x + p.y * p.y);
-      float b0 = (float)q[0], pa = (float)q[1];
+      float b0 = q[0], pa = q[1];
       return f3(b0 * tanf(pa * p.y / r), -b0 * tanf(pa * p.x / r), b0);
     }
     case JSH_B_SPIRAL_CONICAL: {
-      float bz = (float)q[0] / (p.z * p.z);
-      float tp = (float)m.tan_pitch;
+      float bz = q[0] / (p.z * p.z);
+      float tp = X.tan_pitch;
       return f3(bz * (p.x / p.z + p.y * tp), bz * (p.y / p.z - p.x * tp), bz);
     }
     case JSH_B_FORCE_FREE_CYLINDRICAL: {
       float s, c;
       sincos_atan(p.y / p.x, s, c);
-      float b1 = (float)(q[0] * m.bessel1);
-      return f3(-b1 * s, b1 * s, (float)(q[0] * m.bessel0));
+      float b1 = X.b_bessel1;
+      return f3(-b1 * s, b1 * s, X.b_bessel0);
     }
     case JSH_B_HELICAL_CONICAL: {
-      float b = (float)q[0] * fpow(sqrtf(fdot(p, p)), -(float)q[1]);
+      float b = q[0] * fpow(sqrtf(fdot(p, p)), -q[1]);
       float rc2 = p.x * p.x + p.y * p.y;
       float px = 0.f, py = 0.f;
       if (rc2 > 0.f) {
         float irc = rsqrtf(rc2);
         px = -p.y * irc;
         py = p.x * irc;
-        if (q[3] != 0.0 && p.x < 0.f) {
+        if (q[3] != 0.f && p.x < 0.f) {
           px = -px;
           py = -py;
         }
       }
-      float bt = b * (float)m.sin_pitch;
-      return f3(bt * px, bt * py, b * (float)m.cos_pitch);
+      float bt = b * X.sin_pitch;
+      return f3(bt * px, bt * py, b * X.cos_pitch);
     }
     case JSH_B_SIMULATION: {
       float s, c;
@@ -257,15 +260,15 @@ __device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqCons
     nlp = f3(X.nlp[0], X.nlp[1], X.nlp[2]);
     vdir = f3(0, 0, 1);
   } else {
-    Vel v = vfield32(m, p);
+    Vel v = vfield32(m, X, p);
     gamma = v.gamma;
     vdir = v.dir;
     kinematics32(gamma, vdir, f3(X.nl[0], X.nl[1], X.nl[2]), D, nlp, beta);
   }
-  float n = nfield32(m, p);
+  float n = nfield32(m, X, p);
   float np_ = m.n_plasma ? n : n / gamma;
   if (m.b_scalar) {
-    float w = bscalar32(m, p) * D;
+    float w = bscalar32(m, X, p) * D;
     float P = fpow(w, X.pk);
     float Rw = P * rsqrtf(w);
     c.kI = F.ak * np_ * P;
@@ -273,7 +276,7 @@ __device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqCons
     c.kQ = c.kV = c.kF = c.kC = c.eQ = c.eV = 0.f;
     return;
   }
-  F3 B = bvector32(m, p);
+  F3 B = bvector32(m, X, p);
   if (!m.b_plasma) {
     // B' = B / Gamma + Gamma beta^2 / (1 + Gamma) v_hat (v_hat . B)
     B = B * (1.f / gamma) + vdir * (gamma * beta * beta / (1.f + gamma) * fdot(vdir, B));

@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(128) transfer_static64_kernel(const JshRequest
     const JshHit& H = R.hits[h];
     if (R.P.full) transfer_item64<true>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
     else transfer_item64<false>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
+    if (R.P.flags & JSH_FLAG_COST_MAP) o.l = (double)tot.evals;
     write_item(R, f, H.pix, o);
   }
   add_counters(reqs, r, active, tot.evals, tot.acc, tot.rej, o.status);
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(128) transfer_queue64_kernel(const JshRequest*
     else transfer_item64<false>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
     uint64_t q = (uint64_t)f * R.npix + (uint64_t)H.pix;
     if (R.tau) R.tau[q] = o.tau;
-    if (R.l) R.l[q] = o.l;
+    if (R.l) R.l[q] = (R.P.flags & JSH_FLAG_COST_MAP) ? (double)tot.evals : o.l;
     if (R.I) R.I[q] = o.iquv[0];
     if (R.Q) R.Q[q] = o.iquv[1];
     if (R.U) R.U[q] = o.iquv[2];

@@ -69,12 +69,14 @@ struct Lane {
   int8_t first_seg;      // segment where the IQUV pass starts inside (-1: at its end)
   bool init;
   double p0x, p0y, p0z;  // segment start [pc]
+  float bx, by, bz;      // p0 + t d rounded to FP32, refreshed in FP64 when t moves:
+                         // stage points are b + c h d in FP32 (error u |b|)
   double length;         // [pc]
   double length_cm;
   double t, dt;          // [pc]
   double tau_seg, tau_bg, thick;
   double t_first;        // [pc] IQUV start on first_seg: tau_max crossing or optically thick point
-  double chi;
+  double chi;            // Faraday rotation angle, kept reduced to [-pi, pi]
   float x[4];
   float k1[5];
   float s1;  // noise scale of k1
@@ -111,6 +113,9 @@ __device__ __forceinline__ void begin_tau_segment(Lane& L, const JshRequest& R, 
   L.p0x = H.seg[s][0] * INV_PC;
   L.p0y = H.seg[s][1] * INV_PC;
   L.p0z = H.seg[s][2] * INV_PC;
+  L.bx = (float)L.p0x;
+  L.by = (float)L.p0y;
+  L.bz = (float)L.p0z;
   L.t = 0.0;
   L.dt = L.length / R.P.n;
   L.tau_seg = 0.0;
@@ -134,6 +139,9 @@ __device__ __forceinline__ void begin_iquv_segment(Lane& L, const JshRequest& R,
   L.p0x = ox * INV_PC;
   L.p0y = oy * INV_PC;
   L.p0z = oz * INV_PC;
+  L.bx = (float)L.p0x;
+  L.by = (float)L.p0y;
+  L.bz = (float)L.p0z;
   L.t = 0.0;
   L.dt = L.length / first_step_divisor(L.tau_bg, R.P.n);
   L.init = false;
@@ -179,7 +187,7 @@ __device__ __noinline__ void write_finished(const JshRequest* __restrict__ reqs,
   sincos(chi, &ss, &sc);
   double qq = x1, uu = x2;
   if (R.tau) R.tau[q] = tau_bg;
-  if (R.l) R.l[q] = thick;
+  if (R.l) R.l[q] = (R.P.flags & JSH_FLAG_COST_MAP) ? (double)evals : thick;
   if (R.I) R.I[q] = S * (double)x0;
   if (R.Q) R.Q[q] = S * (sc * qq - ss * uu);
   if (R.U) R.U[q] = S * (ss * qq + sc * uu);
@@ -269,17 +277,20 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
   const JshFreqConst F = R.mix.fc[L.f];
   const bool tau = (L.phase == PH_TAU);
   const bool coef_full = FULL && !(tau && warp_tau);
-  const double ddx = tau ? R.plane.dx : -R.plane.dx, ddy = tau ? R.plane.dy : -R.plane.dy,
-               ddz = tau ? R.plane.dz : -R.plane.dz;
-  const F3 dirf = f3((float)ddx, (float)ddy, (float)ddz);
+  // integration direction: +d in the tau pass, -d (towards the observer) after
+  const F3 nl = f3(R.mix.nl[0], R.mix.nl[1], R.mix.nl[2]);
+  const F3 dirf = tau ? f3(-nl.x, -nl.y, -nl.z) : nl;
   const double max_dt = tau ? R.mix.dt_max_pc : 0.0;
   // error-norm tolerances in FP32 (the norm needs a few digits; t and dt stay FP64)
-  const float atol = tau ? (float)R.P.tau_atol : (float)F.atol;
-  const float rtol = tau ? (float)R.P.tau_rtol : (float)R.P.rtol;
+  const float atol = tau ? R.mix.tau_atol : F.atol;
+  const float rtol = tau ? R.mix.tau_rtol : R.mix.rtol;
 
   // integrate_adaptive / adaptive range: finish at exactly t = length
-  if (!(L.length - L.t > DBL_EPSILON)) goto segment_done;
-  if ((L.t + L.dt) - L.length > DBL_EPSILON) L.dt = L.length - L.t;
+  {
+    const double rem = L.length - L.t;
+    if (!(rem > DBL_EPSILON)) goto segment_done;
+    if (L.dt - rem > DBL_EPSILON) L.dt = rem;
+  }
   if (L.nsteps++ >= R.P.max_steps) {
     L.status |= JSH_ST_STEP_LIMIT;
     goto abort;
@@ -294,15 +305,10 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     return;
   }
   {
-    const F3 pn = f3((float)(L.p0x + L.t * ddx), (float)(L.p0y + L.t * ddy), (float)(L.p0z + L.t * ddz));
-    // frame rotation at the step start: chi reduced modulo 2 pi in FP64
-    // (3 FP64 operations), then an FP32 sincos of the reduced angle
+    const F3 pn = f3(L.bx, L.by, L.bz);
+    // frame rotation at the step start: FP32 sincos of the (reduced) angle
     float c0 = 1.f, s0 = 0.f;
-    if (FULL && !tau) {
-      const double two_pi = 6.283185307179586;
-      const float chr = (float)fma(-two_pi, rint(L.chi * (1.0 / two_pi)), L.chi);
-      sincosf(chr, &s0, &c0);
-    }
+    if (FULL && !tau) sincosf((float)L.chi, &s0, &c0);
     const float h = (float)L.dt;
     float dk[5];
     if (!L.init) {
@@ -387,7 +393,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     }
     if (e > 1.0f) {
       float f = 0.9f * __powf(e, -1.0f / 3.0f);
-      L.dt *= (double)(f > 0.2f ? f : 0.2f);
+      L.dt = (double)(h * (f > 0.2f ? f : 0.2f));
       if (max_dt != 0.0 && fabs(L.dt) > max_dt) L.dt = max_dt;
       L.rej++;
       if (++L.fails >= dp::FAIL_LIMIT) {
@@ -404,21 +410,32 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       goto abort;
     }
     L.t = t_new;
+    {
+      const double sg = tau ? 1.0 : -1.0;
+      L.bx = (float)fma(t_new, sg * R.plane.dx, L.p0x);
+      L.by = (float)fma(t_new, sg * R.plane.dy, L.p0y);
+      L.bz = (float)fma(t_new, sg * R.plane.dz, L.p0z);
+    }
     L.fails = 0;
     L.acc++;
     if (e < 0.5f) {
       float ee = e > 0.00032f ? e : 0.00032f;
-      L.dt *= (double)(0.9f * __powf(ee, -0.2f));
+      L.dt = (double)(h * (0.9f * __powf(ee, -0.2f)));
       if (max_dt != 0.0 && fabs(L.dt) > max_dt) L.dt = max_dt;
     }
     if (tau) {
       const double tau_old = L.tau_seg;
       L.tau_seg = tau_old + (double)inc[0];
       if (L.first_seg < 0 && L.tau_bg + L.tau_seg >= R.mix.tau_thick) {
-        // optically thick from here on: the IQUV pass starts at the end of
-        // this step (the tau pass goes on for the tau image)
+        // optically thick from here on: the IQUV pass starts where the
+        // optical depth reaches tau_thick on this step's dense output (to
+        // within 1; a step can span thousands in tau near a jet's core), or
+        // at the step's start if the bisection does not settle; the tau
+        // pass goes on for the tau image
+        double tc = crossing_time(tau_old, t_old, dt_used, h, K(0, 0), K(2, 0), K(3, 0), K(4, 0), K(5, 0),
+                                  K(6, 0), inc[0], R.mix.tau_thick - L.tau_bg, 1.0);
         L.first_seg = L.seg;
-        L.t_first = t_new;
+        L.t_first = tc < 0.0 ? t_old : tc;
       }
       if (L.tau_seg >= R.P.tau_max) {
         L.status |= JSH_ST_TAU_CROSSED;
@@ -441,7 +458,10 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     } else {
 #pragma unroll
       for (int c = 0; c < NX; ++c) L.x[c] += inc[c];
-      if (FULL) L.chi += (double)inc[NK - 1];
+      if (FULL) {
+        L.chi += (double)inc[NK - 1];
+        if (fabs(L.chi) > 3.141592653589793) L.chi = fma(-6.283185307179586, rint(L.chi * 0.15915494309189535), L.chi);
+      }
     }
 #pragma unroll
     for (int c = 0; c < NK; ++c) L.k1[c] = K(6, c);
@@ -618,8 +638,29 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   X.nl[2] = (float)nz;
   X.pk = (float)((s + 2.) / 2.);
   X.dt_max_pc = req->P.dt_max / JSH_PC;
+  X.tau_atol = (float)req->P.tau_atol;
+  X.tau_rtol = (float)req->P.tau_rtol;
+  X.rtol = (float)req->P.rtol;
   X.kq = (float)m.kq_ratio;
   X.eq = (float)m.eq_ratio;
+  for (int i = 0; i < 8; ++i) {
+    X.vq[i] = (float)m.vp[i];
+    X.vq_pc[i] = (float)(m.vp[i] / JSH_PC);
+    X.nq[i] = (float)m.np[i];
+    X.nq_pc[i] = (float)(m.np[i] / JSH_PC);
+    X.bq[i] = (float)m.bp[i];
+    X.bq_pc[i] = (float)(m.bp[i] / JSH_PC);
+  }
+  X.v_dq01 = (float)(m.vp[0] - m.vp[1]);
+  X.v_g0m1 = (float)(m.vp[0] - 1.0);
+  X.v_cone_oz = (float)m.v_cone_oz;
+  X.v_cone_oz_pc = (float)(m.v_cone_oz / JSH_PC);
+  X.v_theta = (float)m.v_theta;
+  X.sin_pitch = (float)m.sin_pitch;
+  X.cos_pitch = (float)m.cos_pitch;
+  X.tan_pitch = (float)m.tan_pitch;
+  X.b_bessel0 = (float)(m.bp[0] * m.bessel0);
+  X.b_bessel1 = (float)(m.bp[0] * m.bessel1);
   // optically thick start of the IQUV pass: the Stokes vector decays at
   // least at rate k_I (1 - |(k_Q, k_U, k_V)| / k_I) along the ray (the
   // symmetric part of the transfer matrix; Faraday terms only rotate), so
@@ -670,7 +711,8 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
     F.c1 = (float)(m.kcr_a * m.kcr_b + m.thermal_fraction);
     F.c2 = (float)(m.kcr_a * Gnu);
     F.scale = S;
-    F.atol = req->P.atol / S;
+    F.atol = (float)(req->P.atol / S);
+    if (F.atol == 0.f && req->P.atol > 0.0) F.atol = FLT_MIN;  // below FP32 range: the smallest normal
     const float vals[6] = {F.ak, F.ae, F.av, F.aev, F.af, F.ac};
     for (float x : vals) {
       if (!isfinite(x) || (x != 0.f && fabsf(x) < 1e-30f)) {

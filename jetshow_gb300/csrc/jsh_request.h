@@ -27,7 +27,8 @@ struct JshParamsDev {
 struct JshFreqConst {
   float ak, ae, av, aev, af, ac, c1, c2;
   double scale;  // S: cgs intensity of one unit of the scaled state
-  double atol;   // I/IQUV-pass atol / S
+  float atol;    // I/IQUV-pass atol / S
+  float pad_;
 };
 
 // Mixed precision, per request.
@@ -41,6 +42,12 @@ struct JshMixed {
   float pad_;
   double dt_max_pc;      // tau-pass step limit [pc], 0 = none
   double tau_thick;      // IQUV pass starts where the optical depth first exceeds this
+  // FP32 copies of the field parameters (q) and of q / pc, and the derived
+  // constants the FP32 field laws use: no FP64 operation per evaluation
+  float vq[8], vq_pc[8], nq[8], nq_pc[8], bq[8], bq_pc[8];
+  float v_dq01, v_g0m1, v_cone_oz, v_cone_oz_pc, v_theta;
+  float sin_pitch, cos_pitch, tan_pitch, b_bessel0, b_bessel1;
+  float tau_atol, tau_rtol, rtol;  // FP32 copies of the step-control tolerances
   const JshFreqConst* fc;  // device [n_nu]
 };
 

@@ -55,6 +55,15 @@ TRANSFER_KW = dict(n=100, tau_max=1e4, tau_min=1e-10, tau_atol=1e-10, tau_rtol=1
 # 1e-7 on tau keeps every sampled pixel within 3e-7 (I) and 2e-6 (tau).
 ACCURATE_KW = dict(n=100, tau_max=1e4, tau_min=1e-10, tau_atol=1e-20, tau_rtol=1e-7, atol=1e-24, rtol=1e-6,
                    output="full")
+# I-only output: the step control sees only I, and rtol 1e-6 leaves FP64 up
+# to 3.6e-4 off the converged I on the conical jet; rtol 1e-7 gives 3.6e-6
+# for 9 % more evaluations.
+ACCURATE_I_KW = dict(ACCURATE_KW, rtol=1e-7, output="I")
+# Gridded fields: the interpolated fields have kinks at every triangle edge
+# and the adaptive steps converge slowly; on the simulation-grid jet FP64 is
+# 2.2e-4 (tau) / 1.3e-4 (I) off a converged solution at ACCURATE_KW and
+# 1.8e-5 / 1.7e-5 at these settings.
+GRID_KW = dict(ACCURATE_KW, tau_rtol=1e-9, rtol=1e-8)
 # Converged reference settings (the FP64 oracle at rtol 1e-10).
 CONVERGED_KW = dict(n=100, tau_max=1e4, tau_min=1e-10, tau_atol=1e-20, tau_rtol=1e-10, atol=1e-30, rtol=1e-10,
                     output="full")
@@ -158,17 +167,24 @@ C3_FIELDS = ("B_p", "B_phi", "n", "Gamma")
 
 def simulation_grid_c3(n_points=200_000, sigma=0.3):
     """The C3 simulation grid: scrambled Sobol points (seed 0) over
-    z in [0, 20] pc, r in [0, 0.5] pc; values B_p, B_phi, n, Gamma of the
+    z in [0, 20] pc, r in [0, 0.5] pc, and the rectangle's edges every
+    0.0125 pc; values B_p, B_phi, n, Gamma of the
     conical jet's laws (B = 0.1 G (R/pc)^-1 split equally poloidal /
-    toroidal, n = 500 (R/pc)^-2, Gamma = 10; R = sqrt(z^2 + r^2)) times
+    toroidal, n = 500 (R/pc)^-2, Gamma = 10; R = sqrt(z^2 + r^2), at least
+    0.005 pc) times
     exp(sigma g) with g the seeded Gaussian random field (correlation
     0.05 pc), FP32.  Returns (xy [n, 2] float64 (z, r) pc, values [n, 4]
     float32)."""
     u = scrambled_sobol2(n_points, seed=0)
-    z, r = 20.0 * u[:, 0], 0.5 * u[:, 1]
+    # plus the domain's edges every 0.0125 pc, so that the hull is the whole
+    # rectangle (the jet axis r = 0 included)
+    ez = np.linspace(0.0, 20.0, 1601)
+    er = np.linspace(0.0, 0.5, 41)[1:-1]
+    z = np.concatenate([20.0 * u[:, 0], ez, ez, np.zeros(er.size), np.full(er.size, 20.0)])
+    r = np.concatenate([0.5 * u[:, 1], np.zeros(ez.size), np.full(ez.size, 0.5), er, er])
     lat, step = gaussian_random_field()
     f = np.exp(sigma * bilinear(lat, step, z, r))
-    R = np.hypot(z, r)
+    R = np.maximum(np.hypot(z, r), 0.005)  # the laws are singular at the apex
     b = 0.1 * (1.0 / R) / math.sqrt(2.0)
     vals = np.column_stack([b * f, b * f, 500.0 * R ** -2 * f, 10.0 * f]).astype(np.float32)
     return np.column_stack([z, r]), vals
@@ -177,11 +193,14 @@ def simulation_grid_c3(n_points=200_000, sigma=0.3):
 def simulation_c3(grid_id: int, scale=1):
     """C3 render on an uploaded C3 grid: Cone (half-angle 0.05) as the
     envelope, every field from the grid (nan_value outside its hull:
-    B = n = 0, Gamma = 1), LOS 0.1 rad, 512x512 uniform pixels of 0.002 mas
-    (the grid's z <= 20 pc projects to 1.08 mas), 15.4 GHz."""
+    B = n = 0, Gamma = 1), LOS 0.1 rad, 512x512 uniform pixels of
+    0.0005 mas, 15.4 GHz.  A ray through the cone at height z spans
+    z/1.5 .. 2z (LOS 0.1, half-angle 0.05); the 0.128 mas half-extent along
+    the jet keeps every ray below z = 9.4 pc, where the cone (r <= 0.47 pc)
+    is inside the grid, so no ray meets the jump to nan_value at the hull."""
     n = max(2, 512 // scale)
     n += n % 2
-    mas = 0.002 * 512 / n
+    mas = 0.0005 * 512 / n
     geo = J.Cone((0, 0, 0), (0, 0, 1), 0.05, 100.0 * J.pc)
     jet = J.Jet(geo, J.SimulationVField(grid_id, 3), J.SimulationBField(grid_id, 0, 1, True),
                 J.SimulationNField(grid_id, 2, True), s=2.5, gamma_min=10.0)

@@ -58,7 +58,8 @@ def test_fp64_vs_converged(ctx, oracle, name):
 
 
 def test_mixed_I_only_vs_converged(ctx, oracle):
-    g, st = gpu(ctx, "c1", "mixed", "persistent", output="I")
+    # I-only output is qualified at rtol 1e-7 (ACCURATE_I_KW)
+    g, st = gpu(ctx, "c1", "mixed", "persistent", output="I", rtol=W.ACCURATE_I_KW["rtol"])
     compare_images(g, converged(oracle, "c1", output="I"), full=False, tau_max=1e4)
 
 
