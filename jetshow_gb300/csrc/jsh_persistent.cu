@@ -45,16 +45,23 @@ namespace {
 constexpr uint8_t PH_IDLE = 0, PH_TAU = 1, PH_IQUV = 2;
 constexpr double INV_PC = 1.0 / JSH_PC;
 
-// Dormand-Prince tableau in FP32: rows 1..6 of a (row 6 = the 5th-order
-// weights b), nodes c, error weights e = b - b_hat, dense-output weights d.
-__constant__ float c_A[7][6] = {
-    {0, 0, 0, 0, 0, 0},
-    {(float)dp::A21, 0, 0, 0, 0, 0},
-    {(float)dp::A31, (float)dp::A32, 0, 0, 0, 0},
-    {(float)dp::A41, (float)dp::A42, (float)dp::A43, 0, 0, 0},
-    {(float)dp::A51, (float)dp::A52, (float)dp::A53, (float)dp::A54, 0, 0},
-    {(float)dp::A61, (float)dp::A62, (float)dp::A63, (float)dp::A64, (float)dp::A65, 0},
-    {(float)dp::B1, 0, (float)dp::B3, (float)dp::B4, (float)dp::B5, (float)dp::B6}};
+// Tableau entry a_sj in FP32 (row 6 = the 5th-order weights b), folded to an
+// immediate operand where s and j are compile-time constants.
+__host__ __device__ constexpr float dp_a32(int s, int j) {
+  return s == 1 ? (j == 0 ? (float)dp::A21 : 0.f)
+       : s == 2 ? (j == 0 ? (float)dp::A31 : j == 1 ? (float)dp::A32 : 0.f)
+       : s == 3 ? (j == 0 ? (float)dp::A41 : j == 1 ? (float)dp::A42 : j == 2 ? (float)dp::A43 : 0.f)
+       : s == 4 ? (j == 0 ? (float)dp::A51 : j == 1 ? (float)dp::A52 : j == 2 ? (float)dp::A53
+                  : j == 3 ? (float)dp::A54 : 0.f)
+       : s == 5 ? (j == 0 ? (float)dp::A61 : j == 1 ? (float)dp::A62 : j == 2 ? (float)dp::A63
+                  : j == 3 ? (float)dp::A64 : j == 4 ? (float)dp::A65 : 0.f)
+       : s == 6 ? (j == 0 ? (float)dp::B1 : j == 2 ? (float)dp::B3 : j == 3 ? (float)dp::B4
+                  : j == 4 ? (float)dp::B5 : j == 5 ? (float)dp::B6 : 0.f)
+       : 0.f;
+}
+
+// Dormand-Prince nodes c, error weights e = b - b_hat and dense-output
+// weights d in FP32.
 __constant__ float c_C[7] = {0, (float)dp::C2, (float)dp::C3, (float)dp::C4, (float)dp::C5, 1.f, 1.f};
 __constant__ float c_E[7] = {(float)dp::E1, 0, (float)dp::E3, (float)dp::E4, (float)dp::E5, (float)dp::E6,
                              (float)dp::E7};
@@ -93,6 +100,31 @@ struct Stages {
     return sh[(s * NK + c) * blockDim.x + threadIdx.x];
   }
 };
+
+// acc = sum_{j < S} a_Sj K_j with S and j compile-time: the tableau entries
+// are immediate operands and the S*NK shared loads are independent.
+template <int S, int NK>
+__device__ __forceinline__ void combine_stage(const Stages<NK>& K, float* acc) {
+#pragma unroll
+  for (int c = 0; c < NK; ++c) acc[c] = 0.f;
+#pragma unroll
+  for (int j = 0; j < S; ++j) {
+#pragma unroll
+    for (int c = 0; c < NK; ++c) acc[c] = fmaf(dp_a32(S, j), K(j, c), acc[c]);
+  }
+}
+
+template <int NK>
+__device__ __forceinline__ void combine(int s, const Stages<NK>& K, float* acc) {
+  switch (s) {
+    case 1: combine_stage<1, NK>(K, acc); break;
+    case 2: combine_stage<2, NK>(K, acc); break;
+    case 3: combine_stage<3, NK>(K, acc); break;
+    case 4: combine_stage<4, NK>(K, acc); break;
+    case 5: combine_stage<5, NK>(K, acc); break;
+    default: combine_stage<6, NK>(K, acc); break;
+  }
+}
 
 __device__ __forceinline__ double seg_len_cm(const JshHit& H, int s, double ox, double oy, double oz) {
   double dx = ox - H.seg[s][0], dy = oy - H.seg[s][1], dz = oz - H.seg[s][2];
@@ -325,13 +357,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
 #pragma unroll 1
     for (int s = 1; s < 7; ++s) {
       float acc[NK];
-#pragma unroll
-      for (int c = 0; c < NK; ++c) acc[c] = 0.f;
-      for (int j = 0; j < s; ++j) {
-        const float a = c_A[s][j];
-#pragma unroll
-        for (int c = 0; c < NK; ++c) acc[c] = fmaf(a, K(j, c), acc[c]);
-      }
+      combine<NK>(s, K, acc);
       float y[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) y[c] = (c < NX) ? fmaf(h, acc[c < NK ? c : 0], L.x[c]) : 0.f;
@@ -664,10 +690,10 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   // optically thick start of the IQUV pass: the Stokes vector decays at
   // least at rate k_I (1 - |(k_Q, k_U, k_V)| / k_I) along the ray (the
   // symmetric part of the transfer matrix; Faraday terms only rotate), so
-  // what enters at optical depth tau_thick is attenuated by exp(-30)
+  // what enters at optical depth tau_thick is attenuated by exp(-20)
   {
     double p = req->P.full ? std::min(0.95, m.kq_ratio + 0.05) : 0.0;
-    double thick = 30.0 / (1.0 - p);
+    double thick = 20.0 / (1.0 - p);
     X.tau_thick = (req->P.flags & JSH_FLAG_IQUV_FROM_TAU_MAX) || !(thick < req->P.tau_max) ? INFINITY : thick;
   }
   if (m.v_kind == JSH_V_CONST_FLAT) {
