@@ -68,6 +68,47 @@ __constant__ float c_E[7] = {(float)dp::E1, 0, (float)dp::E3, (float)dp::E4, (fl
 __constant__ float c_D[7] = {(float)dp::D1, 0, (float)dp::D3, (float)dp::D4, (float)dp::D5, (float)dp::D6,
                              (float)dp::D7};
 
+// Compensated FP32 pair x = hi + lo, |lo| <= ulp(hi) / 2 (about 48 bits):
+// the step-control state (segment coordinate, remainder, optical depth,
+// Faraday angle, base point) is carried in these pairs because GB300 runs
+// FP64 at 1/64 of the FP32 rate; the additions are error-free
+// transformations (Knuth's two-sum, Dekker's product error by fma).
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_of(double x) {
+  const float h = (float)x;
+  return DF{h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ double df_val(DF a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ DF df_norm(float s, float e) {
+  const float hi = s + e;
+  return DF{hi, e - (hi - s)};
+}
+// a + b
+__device__ __forceinline__ DF df_add(DF a, float b) {
+  const float s = a.hi + b;
+  const float bb = s - a.hi;
+  const float e = ((a.hi - (s - bb)) + (b - bb)) + a.lo;
+  return df_norm(s, e);
+}
+// a - b
+__device__ __forceinline__ DF df_sub(DF a, DF b) {
+  const float s = a.hi - b.hi;
+  const float bb = s - a.hi;
+  const float e = ((a.hi - (s - bb)) - (b.hi + bb)) + (a.lo - b.lo);
+  return df_norm(s, e);
+}
+// p + t * d rounded to FP32 (p, t, d pairs)
+__device__ __forceinline__ float df_axpy_round(DF t, DF d, DF p) {
+  const float m = t.hi * d.hi;
+  const float me = fmaf(t.hi, d.hi, -m);  // exact product error
+  const float s = p.hi + m;
+  const float bb = s - p.hi;
+  const float se = (p.hi - (s - bb)) + (m - bb);
+  return s + (((se + me) + p.lo) + fmaf(t.hi, d.lo, t.lo * d.hi));
+}
+
 struct Lane {
   int r, f;
   uint32_t h;
@@ -75,15 +116,18 @@ struct Lane {
   int8_t seg, nseg;
   int8_t first_seg;      // segment where the IQUV pass starts inside (-1: at its end)
   bool init;
-  double p0x, p0y, p0z;  // segment start [pc]
-  float bx, by, bz;      // p0 + t d rounded to FP32, refreshed in FP64 when t moves:
+  bool last;             // dt was truncated to reach the segment's end
+  DF p0x, p0y, p0z;      // segment start [pc]
+  float bx, by, bz;      // p0 + t d rounded to FP32 after each accepted step:
                          // stage points are b + c h d in FP32 (error u |b|)
-  double length;         // [pc]
+  DF length, t;          // segment length and coordinate [pc]
+  float dt;              // [pc]
   double length_cm;
-  double t, dt;          // [pc]
-  double tau_seg, tau_bg, thick;
+  DF tau_seg;            // optical depth of the current tau segment
+  float thick_left;      // tau_thick - (depth of the finished segments)
+  double tau_bg, thick;
   double t_first;        // [pc] IQUV start on first_seg: tau_max crossing or optically thick point
-  double chi;            // Faraday rotation angle, kept reduced to [-pi, pi]
+  DF chi;                // Faraday rotation angle, kept reduced to [-pi, pi]
   float x[4];
   float k1[5];
   float s1;  // noise scale of k1
@@ -138,22 +182,29 @@ __device__ __noinline__ double first_step_divisor(double tau_bg, int n) {
   return auto_n;
 }
 
-__device__ __forceinline__ void begin_tau_segment(Lane& L, const JshRequest& R, const JshHit& H) {
-  int s = L.seg;
-  L.length_cm = seg_len_cm(H, s, H.seg[s][3], H.seg[s][4], H.seg[s][5]);
-  L.length = L.length_cm * INV_PC;
-  L.p0x = H.seg[s][0] * INV_PC;
-  L.p0y = H.seg[s][1] * INV_PC;
-  L.p0z = H.seg[s][2] * INV_PC;
-  L.bx = (float)L.p0x;
-  L.by = (float)L.p0y;
-  L.bz = (float)L.p0z;
-  L.t = 0.0;
-  L.dt = L.length / R.P.n;
-  L.tau_seg = 0.0;
+__device__ __forceinline__ void set_segment(Lane& L, double ox, double oy, double oz, double length_cm) {
+  L.length_cm = length_cm;
+  const double len = length_cm * INV_PC;
+  L.length = df_of(len);
+  L.t = DF{0.f, 0.f};
+  L.p0x = df_of(ox * INV_PC);
+  L.p0y = df_of(oy * INV_PC);
+  L.p0z = df_of(oz * INV_PC);
+  L.bx = L.p0x.hi;
+  L.by = L.p0y.hi;
+  L.bz = L.p0z.hi;
+  L.last = false;
   L.init = false;
   L.nsteps = 0;
   L.fails = 0;
+}
+
+__device__ __forceinline__ void begin_tau_segment(Lane& L, const JshRequest& R, const JshHit& H) {
+  int s = L.seg;
+  set_segment(L, H.seg[s][0], H.seg[s][1], H.seg[s][2], seg_len_cm(H, s, H.seg[s][3], H.seg[s][4], H.seg[s][5]));
+  L.dt = (float)(df_val(L.length) / R.P.n);
+  L.tau_seg = DF{0.f, 0.f};
+  L.thick_left = (float)(R.mix.tau_thick - L.tau_bg);
 }
 
 __device__ __forceinline__ void begin_iquv_segment(Lane& L, const JshRequest& R, const JshHit& H) {
@@ -166,19 +217,8 @@ __device__ __forceinline__ void begin_iquv_segment(Lane& L, const JshRequest& R,
     oy = H.seg[s][1] + R.plane.ry * tc;
     oz = H.seg[s][2] + R.plane.rz * tc;
   }
-  L.length_cm = seg_len_cm(H, s, ox, oy, oz);
-  L.length = L.length_cm * INV_PC;
-  L.p0x = ox * INV_PC;
-  L.p0y = oy * INV_PC;
-  L.p0z = oz * INV_PC;
-  L.bx = (float)L.p0x;
-  L.by = (float)L.p0y;
-  L.bz = (float)L.p0z;
-  L.t = 0.0;
-  L.dt = L.length / first_step_divisor(L.tau_bg, R.P.n);
-  L.init = false;
-  L.nsteps = 0;
-  L.fails = 0;
+  set_segment(L, ox, oy, oz, seg_len_cm(H, s, ox, oy, oz));
+  L.dt = (float)(df_val(L.length) / first_step_divisor(L.tau_bg, R.P.n));
 }
 
 __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict__ reqs,
@@ -198,7 +238,7 @@ __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict
   L.tau_bg = 0.0;
   L.thick = 0.0;
   L.t_first = -1.0;
-  L.chi = 0.0;
+  L.chi = DF{0.f, 0.f};
   L.x[0] = L.x[1] = L.x[2] = L.x[3] = 0.f;
   L.status = (uint32_t)H.status | JSH_ST_HIT;
   L.evals = L.acc = L.rej = 0;
@@ -233,8 +273,8 @@ __device__ __noinline__ void write_finished(const JshRequest* __restrict__ reqs,
 }
 
 __device__ __forceinline__ void lane_finish(Lane& L, const JshRequest* __restrict__ reqs) {
-  write_finished(reqs, L.r, L.f, L.h, L.tau_bg, L.thick, L.chi, L.x[0], L.x[1], L.x[2], L.x[3], L.status, L.evals,
-                 L.acc, L.rej);
+  write_finished(reqs, L.r, L.f, L.h, L.tau_bg, L.thick, df_val(L.chi), L.x[0], L.x[1], L.x[2], L.x[3], L.status,
+                 L.evals, L.acc, L.rej);
   L.phase = PH_IDLE;
 }
 
@@ -312,22 +352,25 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
   // integration direction: +d in the tau pass, -d (towards the observer) after
   const F3 nl = f3(R.mix.nl[0], R.mix.nl[1], R.mix.nl[2]);
   const F3 dirf = tau ? f3(-nl.x, -nl.y, -nl.z) : nl;
-  const double max_dt = tau ? R.mix.dt_max_pc : 0.0;
+  const float max_dt = tau ? R.mix.dt_max_f : 0.f;
   // error-norm tolerances in FP32 (the norm needs a few digits; t and dt stay FP64)
   const float atol = tau ? R.mix.tau_atol : F.atol;
   const float rtol = tau ? R.mix.tau_rtol : R.mix.rtol;
 
-  // integrate_adaptive / adaptive range: finish at exactly t = length
+  // integrate_adaptive / adaptive range: finish at exactly t = length (a
+  // step that would pass the end is shortened to end there)
   {
-    const double rem = L.length - L.t;
-    if (!(rem > DBL_EPSILON)) goto segment_done;
-    if (L.dt - rem > DBL_EPSILON) L.dt = rem;
+    const DF rem = df_sub(L.length, L.t);
+    const float remf = rem.hi + rem.lo;
+    if (!(remf > 0.f)) goto segment_done;
+    L.last = !(L.dt < remf);
+    if (L.last) L.dt = remf;
   }
   if (L.nsteps++ >= R.P.max_steps) {
     L.status |= JSH_ST_STEP_LIMIT;
     goto abort;
   }
-  if (max_dt != 0.0 && fabs(L.dt) > max_dt) {
+  if (max_dt != 0.f && fabsf(L.dt) > max_dt) {
     L.dt = max_dt;
     L.rej++;
     if (++L.fails >= dp::FAIL_LIMIT) {
@@ -340,8 +383,8 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     const F3 pn = f3(L.bx, L.by, L.bz);
     // frame rotation at the step start: FP32 sincos of the (reduced) angle
     float c0 = 1.f, s0 = 0.f;
-    if (FULL && !tau) sincosf((float)L.chi, &s0, &c0);
-    const float h = (float)L.dt;
+    if (FULL && !tau) sincosf(L.chi.hi, &s0, &c0);
+    const float h = L.dt;
     float dk[5];
     if (!L.init) {
       L.s1 = rhs32(R, F, tau, coef_full, pn, L.x, c0, s0, dk);
@@ -397,7 +440,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     float e;
     if (tau) {
       // no cancellation in dtau/dt = k_I: the plain odeint norm
-      e = fabsf(err[0]) / fmaf(rtol, fmaf(adt, fabsf(L.k1[0]), fabsf((float)L.tau_seg)), atol);
+      e = fabsf(err[0]) / fmaf(rtol, fmaf(adt, fabsf(L.k1[0]), fabsf(L.tau_seg.hi)), atol);
     } else {
       e = 0.f;
 #pragma unroll
@@ -419,8 +462,8 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     }
     if (e > 1.0f) {
       float f = 0.9f * __powf(e, -1.0f / 3.0f);
-      L.dt = (double)(h * (f > 0.2f ? f : 0.2f));
-      if (max_dt != 0.0 && fabs(L.dt) > max_dt) L.dt = max_dt;
+      L.dt = h * (f > 0.2f ? f : 0.2f);
+      if (max_dt != 0.f && fabsf(L.dt) > max_dt) L.dt = max_dt;
       L.rej++;
       if (++L.fails >= dp::FAIL_LIMIT) {
         L.status |= JSH_ST_FAIL_LIMIT;
@@ -429,55 +472,57 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       return;
     }
     // accept
-    const double t_old = L.t, dt_used = L.dt;
-    const double t_new = L.t + L.dt;
-    if (t_new == L.t) {
+    const DF t_prev = L.t;
+    const DF t_new = L.last ? L.length : df_add(L.t, h);
+    if (t_new.hi == t_prev.hi && t_new.lo == t_prev.lo) {
       L.status |= JSH_ST_DT_UNDERFLOW;
       goto abort;
     }
     L.t = t_new;
     {
-      const double sg = tau ? 1.0 : -1.0;
-      L.bx = (float)fma(t_new, sg * R.plane.dx, L.p0x);
-      L.by = (float)fma(t_new, sg * R.plane.dy, L.p0y);
-      L.bz = (float)fma(t_new, sg * R.plane.dz, L.p0z);
+      const float sg = tau ? 1.f : -1.f;
+      L.bx = df_axpy_round(t_new, DF{sg * R.mix.dhi[0], sg * R.mix.dlo[0]}, L.p0x);
+      L.by = df_axpy_round(t_new, DF{sg * R.mix.dhi[1], sg * R.mix.dlo[1]}, L.p0y);
+      L.bz = df_axpy_round(t_new, DF{sg * R.mix.dhi[2], sg * R.mix.dlo[2]}, L.p0z);
     }
     L.fails = 0;
     L.acc++;
     if (e < 0.5f) {
       float ee = e > 0.00032f ? e : 0.00032f;
-      L.dt = (double)(h * (0.9f * __powf(ee, -0.2f)));
-      if (max_dt != 0.0 && fabs(L.dt) > max_dt) L.dt = max_dt;
+      L.dt = h * (0.9f * __powf(ee, -0.2f));
+      if (max_dt != 0.f && fabsf(L.dt) > max_dt) L.dt = max_dt;
     }
     if (tau) {
-      const double tau_old = L.tau_seg;
-      L.tau_seg = tau_old + (double)inc[0];
-      if (L.first_seg < 0 && L.tau_bg + L.tau_seg >= R.mix.tau_thick) {
+      const DF tau_prev = L.tau_seg;
+      L.tau_seg = df_add(L.tau_seg, inc[0]);
+      if (L.first_seg < 0 && L.tau_seg.hi >= L.thick_left) {
         // optically thick from here on: the IQUV pass starts where the
         // optical depth reaches tau_thick on this step's dense output (to
         // within 1; a step can span thousands in tau near a jet's core), or
         // at the step's start if the bisection does not settle; the tau
         // pass goes on for the tau image
-        double tc = crossing_time(tau_old, t_old, dt_used, h, K(0, 0), K(2, 0), K(3, 0), K(4, 0), K(5, 0),
-                                  K(6, 0), inc[0], R.mix.tau_thick - L.tau_bg, 1.0);
+        const double t_old = df_val(t_prev);
+        double tc = crossing_time(df_val(tau_prev), t_old, (double)h, h, K(0, 0), K(2, 0), K(3, 0), K(4, 0),
+                                  K(5, 0), K(6, 0), inc[0], R.mix.tau_thick - L.tau_bg, 1.0);
         L.first_seg = L.seg;
         L.t_first = tc < 0.0 ? t_old : tc;
       }
-      if (L.tau_seg >= R.P.tau_max) {
+      if (L.tau_seg.hi > R.mix.tau_max_hi || (L.tau_seg.hi == R.mix.tau_max_hi && L.tau_seg.lo >= R.mix.tau_max_lo)) {
         L.status |= JSH_ST_TAU_CROSSED;
-        double tc = crossing_time(tau_old, t_old, dt_used, h, K(0, 0), K(2, 0), K(3, 0), K(4, 0), K(5, 0),
-                                  K(6, 0), inc[0], R.P.tau_max, R.P.tau_precision);
+        const double t_old = df_val(t_prev);
+        double tc = crossing_time(df_val(tau_prev), t_old, (double)h, h, K(0, 0), K(2, 0), K(3, 0), K(4, 0),
+                                  K(5, 0), K(6, 0), inc[0], R.P.tau_max, R.P.tau_precision);
         if (tc < 0.0) {
           // the reference keeps bisecting; stop at the last bracket's midpoint
           L.status |= JSH_ST_BISECT_LIMIT;
-          tc = t_old + 0.5 * dt_used;
+          tc = t_old + 0.5 * (double)h;
         }
         if (L.first_seg < 0 || (L.first_seg == L.seg && tc < L.t_first)) {
           L.first_seg = L.seg;
           L.t_first = tc;
         }
         L.nseg = L.seg + 1;
-        L.tau_bg += L.tau_seg;
+        L.tau_bg += df_val(L.tau_seg);
         L.thick += L.length_cm;
         goto start_iquv;
       }
@@ -485,8 +530,14 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
 #pragma unroll
       for (int c = 0; c < NX; ++c) L.x[c] += inc[c];
       if (FULL) {
-        L.chi += (double)inc[NK - 1];
-        if (fabs(L.chi) > 3.141592653589793) L.chi = fma(-6.283185307179586, rint(L.chi * 0.15915494309189535), L.chi);
+        L.chi = df_add(L.chi, inc[NK - 1]);
+        if (fabsf(L.chi.hi) > 3.14159265f) {
+          // subtract k 2 pi exactly: 2 pi = c_hi + c_lo, k c_hi = p + pe
+          const float k = rintf(L.chi.hi * 0.159154943f);
+          const float c_hi = 6.28318548f, c_lo = -1.74845553e-7f;
+          const float pr = k * c_hi, pe = fmaf(k, c_hi, -pr);
+          L.chi = df_add(df_add(L.chi, -pr), -fmaf(k, c_lo, pe));
+        }
       }
     }
 #pragma unroll
@@ -498,7 +549,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
 segment_done : {
   const JshHit& H = R.hits[L.h];
   if (tau) {
-    L.tau_bg += L.tau_seg;
+    L.tau_bg += df_val(L.tau_seg);
     L.thick += L.length_cm;
     if (L.seg + 1 < L.nseg) {
       L.seg++;
@@ -530,7 +581,7 @@ start_iquv : {
 
 abort:
   if (tau) {
-    L.tau_bg += L.tau_seg;
+    L.tau_bg += df_val(L.tau_seg);
     L.thick += L.length_cm;
   }
   lane_finish(L, reqs);
@@ -554,7 +605,7 @@ __global__ void __launch_bounds__(128) transfer_static_mixed_kernel(const JshReq
 // Persistent CTAs: each warp keeps 32 lanes busy, refilling idle lanes from
 // the global queue when at least `refill` of them are idle.
 template <bool FULL>
-__global__ void __launch_bounds__(256) transfer_persistent_mixed_kernel(const JshRequest* __restrict__ reqs,
+__global__ void __launch_bounds__(256, 1) transfer_persistent_mixed_kernel(const JshRequest* __restrict__ reqs,
                                                                          int n_req, unsigned long long* queue,
                                                                          int refill) {
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
@@ -664,6 +715,16 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   X.nl[2] = (float)nz;
   X.pk = (float)((s + 2.) / 2.);
   X.dt_max_pc = req->P.dt_max / JSH_PC;
+  X.dt_max_f = (float)X.dt_max_pc;
+  {
+    const double d[3] = {req->plane.dx, req->plane.dy, req->plane.dz};
+    for (int k = 0; k < 3; ++k) {
+      X.dhi[k] = (float)d[k];
+      X.dlo[k] = (float)(d[k] - (double)X.dhi[k]);
+    }
+    X.tau_max_hi = (float)req->P.tau_max;
+    X.tau_max_lo = (float)(req->P.tau_max - (double)X.tau_max_hi);
+  }
   X.tau_atol = (float)req->P.tau_atol;
   X.tau_rtol = (float)req->P.tau_rtol;
   X.rtol = (float)req->P.rtol;

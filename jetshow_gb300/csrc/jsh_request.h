@@ -48,6 +48,9 @@ struct JshMixed {
   float v_dq01, v_g0m1, v_cone_oz, v_cone_oz_pc, v_theta;
   float sin_pitch, cos_pitch, tan_pitch, b_bessel0, b_bessel1;
   float tau_atol, tau_rtol, rtol;  // FP32 copies of the step-control tolerances
+  float dt_max_f;                  // dt_max_pc in FP32
+  float dhi[3], dlo[3];            // ray direction as compensated FP32 pairs
+  float tau_max_hi, tau_max_lo;    // tau_max as a compensated FP32 pair
   const JshFreqConst* fc;  // device [n_nu]
 };
 
