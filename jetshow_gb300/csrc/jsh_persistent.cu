@@ -766,6 +766,7 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
     double D = 1. / (gamma * (1. - beta * nz));
     double f = (D + 1.) * (gamma / (gamma + 1.));
     X.v_const = 1;
+    X.helical_bk = (m.b_kind == JSH_B_HELICAL_CONICAL && m.n_kind == JSH_N_BK) ? 1 : 0;
     X.D = (float)D;
     X.gamma = (float)gamma;
     X.beta = (float)beta;
