@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=int, default=1, help="shrink the image (debug only)")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-gridded", dest="gridded", action="store_false",
+                    help="skip the simulation-grid leg")
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests of the replayed serving stream (0 skips the serving leg)")
     return ap.parse_args()
@@ -235,6 +237,39 @@ def serving_leg(ctx, n_requests):
             "tolerances": "rtol 1e-6 / 1e-7 tau, atol 1e-24 / 1e-20 tau, mixed precision, full Stokes"}
 
 
+def gridded_leg(ctx, steps=3):
+    """The simulation-grid jet (203 284-point triangulated grid, 512x512 at
+    15.4 GHz, every field interpolated on the device): host triangulation
+    and upload time, then the batched and plain forms (device time per
+    render)."""
+    from jetshow_gb300 import jet as J
+    from jetshow_gb300 import workloads as W
+    from jetshow_gb300.runtime import triangulate
+    t0 = time.perf_counter()
+    xy, vals = W.simulation_grid_c3()
+    tri = triangulate(xy)
+    t1 = time.perf_counter()
+    gid = ctx.grid_upload(xy, vals, tri)
+    t2 = time.perf_counter()
+    jet, plane, nu, _ = W.simulation_c3(gid)
+    out = {"grid_points": int(xy.shape[0]), "triangles": int(tri.shape[0]), "triangulate_s": t1 - t0,
+           "upload_s": t2 - t1, "image": list(plane.image_size), "n_freq": int(nu.size),
+           "l2": "not flushed: the 13 MB grid is meant to stay resident in the 129 MB L2"}
+    for name, kw in (("batched", dict(precision="mixed", schedule="persistent")),
+                     ("plain_fp64", dict(precision="fp64", schedule="static"))):
+        p = J.make_params(**kw, **W.ACCURATE_KW)
+        if name == "batched":
+            ctx.autotune(jet.desc(), plane.desc(), nu, p)
+        ms = []
+        for i in range(1 + (steps if name == "batched" else 1)):
+            _, st = ctx.render(jet.desc(), plane.desc(), nu, p)
+            if i > 0:
+                ms.append(st["device_ms"])
+        out[name] = {"rays_per_s": st["n_work_items"] / (np.mean(ms) * 1e-3), "ms": float(np.mean(ms)),
+                     "work_items": int(st["n_work_items"]), "rhs_evals": int(st["rhs_evals"])}
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -354,6 +389,7 @@ def main():
             "fp64_peak_tflops": peaks["fp64_tflops"]}
     cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 else None
     serving = serving_leg(ctx, args.serve_requests) if args.serve_requests > 0 else None
+    gridded = gridded_leg(ctx) if args.gridded else None
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -372,6 +408,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": float(np.mean(e2e_ms))},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
+                "gridded": gridded,
                 "gpu_launches": 4, "autotuned_shape": tuning, "rhs_evals_per_step": st_b["rhs_evals"],
                 "steps_accepted": st_b["steps_accepted"], "steps_rejected": st_b["steps_rejected"]}
         print(json.dumps(line), flush=True)

@@ -67,6 +67,8 @@ void jsh_request_layout(uint64_t npix, uint64_t n_along, uint64_t n_across, int3
   o = align_up(o + sizeof(uint32_t));
   L->off_queue = o;
   o = align_up(o + sizeof(uint32_t));
+  L->off_buckets = o;
+  o = align_up(o + sizeof(uint32_t) * JSH_RANK_BUCKETS * 2);
   L->off_nu = o;
   o = align_up(o + sizeof(double) * n_nu);
   L->off_fc = o;
@@ -79,6 +81,10 @@ void jsh_request_layout(uint64_t npix, uint64_t n_along, uint64_t n_across, int3
   o = align_up(o + sizeof(double) * (n_across / 2) * n_along);
   L->off_hits = o;
   o = align_up(o + sizeof(JshHit) * npix);
+  L->off_order = o;
+  o = align_up(o + sizeof(uint32_t) * npix);
+  L->off_key = o;
+  o = align_up(o + npix);
   L->own_outputs = own_outputs;
   for (int k = 0; k < 7; ++k) {
     L->off_out[k] = o;
@@ -96,6 +102,9 @@ void jsh_bind_request(JshRequest* req, char* base, const JshRequestLayout& L, bo
   req->plane.along_center = (double*)(base + L.off_along_center);
   req->plane.across_pos = (double*)(base + L.off_across);
   req->hits = (JshHit*)(base + L.off_hits);
+  req->buckets = (uint32_t*)(base + L.off_buckets);
+  req->order = (uint32_t*)(base + L.off_order);
+  req->key = (uint8_t*)(base + L.off_key);
   if (own_outputs) {
     req->tau = (double*)(base + L.off_out[0]);
     req->l = (double*)(base + L.off_out[1]);
@@ -324,7 +333,7 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
   JSH_CUDA_TRY(jsh_launch_hit(d_req, 1, npix, stream));
   JshLaunchShape shape = jsh_effective_shape(ctx, params);
   JSH_CUDA_TRY(jsh_launch_transfer(d_req, 1, params->precision, params->schedule, params->output == JSH_OUT_FULL,
-                                   npix * (uint64_t)n_nu, shape, (unsigned int*)(base + L.off_queue),
+                                   npix * (uint64_t)n_nu, npix, shape, (unsigned int*)(base + L.off_queue),
                                    ctx->num_sms, stream));
   JSH_CUDA_TRY(cudaEventRecord(ctx->ws_ready, stream));
   ctx->last_pending = true;

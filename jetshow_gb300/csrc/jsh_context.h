@@ -28,8 +28,8 @@ struct JshGridSlot {
 
 // Layout of one request's device memory inside an arena allocation.
 struct JshRequestLayout {
-  size_t off_req, off_counters, off_nhit, off_queue, off_nu, off_fc, off_along_size, off_along_center, off_across,
-      off_hits, off_out[7];
+  size_t off_req, off_counters, off_nhit, off_queue, off_buckets, off_nu, off_fc, off_along_size, off_along_center,
+      off_across, off_hits, off_order, off_key, off_out[7];
   size_t total;
   bool own_outputs;
 };

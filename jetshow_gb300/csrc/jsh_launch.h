@@ -27,10 +27,11 @@ cudaError_t jsh_launch_hit(const JshRequest* d_reqs, int n_req, uint64_t max_pix
 
 // Transfer every (hit ray, frequency) of the batch.  `queue` is a zeroed
 // device counter used by the persistent schedule; max_items bounds the
-// total work items (sum of npix * n_nu) for the static grid.
+// total work items (sum of npix * n_nu) for the static grid, max_hits the
+// hit rays of one request.
 cudaError_t jsh_launch_transfer(const JshRequest* d_reqs, int n_req, int precision, int schedule, bool full,
-                                uint64_t max_items, const JshLaunchShape& shape, unsigned int* queue,
-                                int num_sms, cudaStream_t stream);
+                                uint64_t max_items, uint64_t max_hits, const JshLaunchShape& shape,
+                                unsigned int* queue, int num_sms, cudaStream_t stream);
 
 // Hit arbitrary rays (origins/directions device arrays, directions already
 // normalised on the device by this kernel as Ray::Ray does).

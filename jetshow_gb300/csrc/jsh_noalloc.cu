@@ -150,7 +150,7 @@ extern "C" int jsh_observation_run_noalloc(const jsh_model_desc* model, const js
                        params->ctas_per_sm, params->refill_threshold > 0 ? params->refill_threshold : 8};
   shape.block_size = shape.block_size < 32 ? 32 : (shape.block_size > 256 ? 256 : shape.block_size / 32 * 32);
   JSH_CUDA_TRY(jsh_launch_transfer(d_req, 1, params->precision, params->schedule,
-                                   params->output == JSH_OUT_FULL, npix * (uint64_t)n_nu, shape,
+                                   params->output == JSH_OUT_FULL, npix * (uint64_t)n_nu, npix, shape,
                                    (unsigned int*)(base + L.off_queue), sms, s));
   return JSH_OK;
 }

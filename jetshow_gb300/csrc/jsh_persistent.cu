@@ -221,15 +221,25 @@ __device__ __forceinline__ void begin_iquv_segment(Lane& L, const JshRequest& R,
   L.dt = (float)(df_val(L.length) / first_step_divisor(L.tau_bg, R.P.n));
 }
 
+// Work item w of the batch.  Unranked: frequency-major over the hit list.
+// Ranked (persistent schedule): all frequencies of a ray together, rays in
+// the heaviest-first order of the ranking kernels.
 __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict__ reqs,
-                                           const unsigned long long* base, int n_req, unsigned long long w) {
+                                           const unsigned long long* base, int n_req, unsigned long long w,
+                                           bool ranked) {
   int r = find_request(base, n_req, w);
   const JshRequest& R = reqs[r];
   unsigned long long local = w - base[r];
-  unsigned nhit = *R.n_hit;
   L.r = r;
-  L.f = (int)(local / nhit);
-  L.h = (uint32_t)(local % nhit);
+  if (ranked) {
+    const unsigned long long rank = local / (unsigned)R.n_nu;
+    L.f = (int)(local - rank * (unsigned)R.n_nu);
+    L.h = R.order[rank];
+  } else {
+    unsigned nhit = *R.n_hit;
+    L.f = (int)(local / nhit);
+    L.h = (uint32_t)(local % nhit);
+  }
   const JshHit& H = R.hits[L.h];
   L.phase = PH_TAU;
   L.seg = 0;
@@ -587,6 +597,78 @@ abort:
   lane_finish(L, reqs);
 }
 
+// ------------------------------------------------------------- ranking
+// Heaviest-first order of the hit rays for the persistent schedule.  A ray's
+// cost grows with its optical depth (up to the optically thick start of the
+// IQUV pass): rays through the core take thousands of steps, rays far out a
+// few hundred.  So each ray's optical depth at the request's first
+// frequency is estimated (4-point Gauss-Legendre over each segment, the FP32
+// coefficients), bucketed by factors of 2 and counting-sorted in descending
+// order; the queue then hands out the heaviest rays first and they run while
+// the bulk fills the GPU, instead of starting late and setting the render's
+// makespan.
+__global__ void __launch_bounds__(256) rank_cost_kernel(const JshRequest* __restrict__ reqs) {
+  __shared__ uint32_t hist[JSH_RANK_BUCKETS];
+  const JshRequest& R = reqs[blockIdx.y];
+  for (int b = threadIdx.x; b < JSH_RANK_BUCKETS; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
+  const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h < *R.n_hit) {
+    const JshHit& H = R.hits[h];
+    const JshFreqConst F = R.mix.fc[0];
+    const float xk[4] = {0.0694318442f, 0.330009478f, 0.669990522f, 0.930568156f};
+    const float wk[4] = {0.173927423f, 0.326072577f, 0.326072577f, 0.173927423f};
+    float tau = 0.f;
+    for (int s = 0; s < H.nseg && s < 2; ++s) {
+      const F3 a = f3((float)(H.seg[s][0] * INV_PC), (float)(H.seg[s][1] * INV_PC), (float)(H.seg[s][2] * INV_PC));
+      const F3 b = f3((float)(H.seg[s][3] * INV_PC), (float)(H.seg[s][4] * INV_PC), (float)(H.seg[s][5] * INV_PC));
+      const F3 d = b - a;
+      float acc = 0.f;
+#pragma unroll 1
+      for (int k = 0; k < 4; ++k) {
+        Coef32 c;
+        coef32_rt(R, F, a + d * xk[k], false, c);
+        acc = fmaf(wk[k], c.kI, acc);
+      }
+      tau = fmaf(acc, sqrtf(fdot(d, d)), tau);
+    }
+    int key = 0;
+    if (tau > 0.f && tau < INFINITY) key = min(max((int)floorf(__log2f(tau)) + 40, 1), JSH_RANK_BUCKETS - 1);
+    R.key[h] = (uint8_t)key;
+    atomicAdd(&hist[key], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < JSH_RANK_BUCKETS; b += blockDim.x)
+    if (hist[b]) atomicAdd(&R.buckets[b], hist[b]);
+}
+
+// Start of each bucket in descending bucket order (one thread per request).
+__global__ void rank_prefix_kernel(const JshRequest* __restrict__ reqs) {
+  const JshRequest& R = reqs[blockIdx.x];
+  if (threadIdx.x != 0) return;
+  uint32_t run = 0;
+  for (int b = JSH_RANK_BUCKETS - 1; b >= 0; --b) {
+    R.buckets[JSH_RANK_BUCKETS + b] = run;
+    run += R.buckets[b];
+  }
+}
+
+// order[position] = hit index; the lanes of a warp with the same bucket take
+// consecutive positions with one atomic.
+__global__ void __launch_bounds__(256) rank_scatter_kernel(const JshRequest* __restrict__ reqs) {
+  const JshRequest& R = reqs[blockIdx.y];
+  const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= *R.n_hit) return;
+  const int key = R.key[h];
+  const unsigned peers = __match_any_sync(__activemask(), key);
+  const int leader = __ffs(peers) - 1;
+  const unsigned lane = threadIdx.x & 31u;
+  uint32_t base = 0;
+  if ((int)lane == leader) base = atomicAdd(&R.buckets[JSH_RANK_BUCKETS + key], (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  R.order[base + __popc(peers & ((1u << lane) - 1u))] = h;
+}
+
 // One thread per work item, stepped to completion.
 template <bool FULL>
 __global__ void __launch_bounds__(128) transfer_static_mixed_kernel(const JshRequest* __restrict__ reqs,
@@ -598,7 +680,7 @@ __global__ void __launch_bounds__(128) transfer_static_mixed_kernel(const JshReq
   if (w >= base[n_req]) return;
   const Stages<FULL ? 5 : 1> K{ksh};
   Lane L;
-  lane_start(L, reqs, base, n_req, w);
+  lane_start(L, reqs, base, n_req, w, false);
   while (L.phase != PH_IDLE) lane_step<FULL>(L, reqs, L.phase == PH_TAU, K);
 }
 
@@ -628,7 +710,7 @@ __global__ void __launch_bounds__(256, 1) transfer_persistent_mixed_kernel(const
       if (b + (unsigned long long)nidle >= total) exhausted = true;
       if (L.phase == PH_IDLE) {
         unsigned long long w = b + (unsigned long long)__popc(idle & lt_mask);
-        if (w < total) lane_start(L, reqs, base, n_req, w);
+        if (w < total) lane_start(L, reqs, base, n_req, w, true);
       }
     }
     unsigned active = __ballot_sync(0xffffffffu, L.phase != PH_IDLE);
@@ -653,8 +735,8 @@ constexpr size_t stage_smem(int block) {
 using namespace jsh;
 
 cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int schedule, bool full,
-                                      uint64_t max_items, const JshLaunchShape& shape, unsigned int* queue,
-                                      int num_sms, cudaStream_t stream) {
+                                      uint64_t max_items, uint64_t max_hits, const JshLaunchShape& shape,
+                                      unsigned int* queue, int num_sms, cudaStream_t stream) {
   if (schedule == JSH_SCHED_STATIC) {
     const int bs = 128;
     unsigned blocks = (unsigned)((max_items + bs - 1) / bs);
@@ -663,6 +745,12 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
     else
       transfer_static_mixed_kernel<false><<<blocks, bs, stage_smem<false>(bs), stream>>>(d_reqs, n_req);
     return cudaGetLastError();
+  }
+  if (max_hits > 0) {
+    const dim3 g((unsigned)((max_hits + 255) / 256), (unsigned)n_req);
+    rank_cost_kernel<<<g, 256, 0, stream>>>(d_reqs);
+    rank_prefix_kernel<<<n_req, 32, 0, stream>>>(d_reqs);
+    rank_scatter_kernel<<<g, 256, 0, stream>>>(d_reqs);
   }
   int bs = shape.block_size;
   if (bs > 256) bs = 256;

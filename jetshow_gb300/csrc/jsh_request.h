@@ -14,6 +14,9 @@ struct JshHit {           // one intersecting pixel (Intersection list)
   double seg[JSH_MAX_SEG][6];  // {point_in xyz, point_out xyz}
 };
 
+// Cost buckets of the heaviest-first ranking (factors of 2 in optical depth).
+#define JSH_RANK_BUCKETS 64
+
 struct JshParamsDev {
   int32_t n, full, precision, schedule, flags, pad_;
   double tau_max, tau_min, dt_max;
@@ -61,6 +64,12 @@ struct JshRequest {
   JshPlane plane;
   JshParamsDev P;
   JshHit* hits;           // device [npix] (first n_hit valid)
+  // persistent mixed schedule: hit rays ranked by estimated cost, heaviest
+  // first (order[rank] = hit index), their cost buckets and the bucket
+  // counts / cursors [2][JSH_RANK_BUCKETS] (zeroed with the counters)
+  uint32_t* order;
+  uint8_t* key;
+  uint32_t* buckets;
   uint32_t* n_hit;        // device counter written by the hit kernel
   const double* nu;       // device [n_nu] source-frame frequencies
   int32_t n_nu;

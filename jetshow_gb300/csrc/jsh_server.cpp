@@ -157,10 +157,12 @@ struct jsh_server {
 
 namespace {
 
-// Counters region of slot s: [JSH_MAX_BATCH][8] u64 + n_hit[JSH_MAX_BATCH] + queue.
+// Counters region of slot s: [JSH_MAX_BATCH][8] u64 counters, n_hit[JSH_MAX_BATCH],
+// [JSH_MAX_BATCH][2][JSH_RANK_BUCKETS] rank buckets, then the queue counter.
+size_t nhit_off() { return align_up(sizeof(unsigned long long) * 8 * JSH_MAX_BATCH); }
+size_t buckets_off() { return nhit_off() + align_up(sizeof(uint32_t) * JSH_MAX_BATCH); }
 size_t counters_region_bytes() {
-  return align_up(sizeof(unsigned long long) * 8 * JSH_MAX_BATCH) + align_up(sizeof(uint32_t) * JSH_MAX_BATCH) +
-         256;
+  return buckets_off() + align_up(sizeof(uint32_t) * 2 * JSH_RANK_BUCKETS * JSH_MAX_BATCH) + 256;
 }
 
 int prepare_request(jsh_server* S, Request* q) {
@@ -188,9 +190,10 @@ void bind(jsh_server* S, Slot& sl, Request* q, int i) {
   jsh_bind_request(&r, blk, q->L, true);
   char* ctl = sl.dev;
   unsigned long long* counters = (unsigned long long*)(ctl + sl.counters_off);
-  uint32_t* nhit = (uint32_t*)(ctl + sl.counters_off + align_up(sizeof(unsigned long long) * 8 * JSH_MAX_BATCH));
+  uint32_t* nhit = (uint32_t*)(ctl + sl.counters_off + nhit_off());
   r.counters = counters + 8 * i;
   r.n_hit = nhit + i;
+  r.buckets = (uint32_t*)(ctl + sl.counters_off + buckets_off()) + 2 * JSH_RANK_BUCKETS * i;
   r.nu = (const double*)(ctl + offsetof(SlotHost, nu) + sizeof(double) * JSH_SERVER_MAX_NU * i);
   r.mix.fc = (const JshFreqConst*)(ctl + offsetof(SlotHost, fc) + sizeof(JshFreqConst) * JSH_SERVER_MAX_NU * i);
   sl.host->recs[i] = r;
@@ -206,9 +209,10 @@ void bind_empty(Slot& sl, int i) {
   memset(&r, 0, sizeof(r));
   char* ctl = sl.dev;
   unsigned long long* counters = (unsigned long long*)(ctl + sl.counters_off);
-  uint32_t* nhit = (uint32_t*)(ctl + sl.counters_off + align_up(sizeof(unsigned long long) * 8 * JSH_MAX_BATCH));
+  uint32_t* nhit = (uint32_t*)(ctl + sl.counters_off + nhit_off());
   r.counters = counters + 8 * i;
   r.n_hit = nhit + i;
+  r.buckets = (uint32_t*)(ctl + sl.counters_off + buckets_off()) + 2 * JSH_RANK_BUCKETS * i;
   r.plane.n_across = 2;
   r.plane.n_along = 0;
   sl.host->recs[i] = r;
@@ -229,7 +233,8 @@ cudaError_t enqueue_slot(jsh_server* S, Slot& sl, int n_req, bool full) {
   JshLaunchShape shape = S->ctx->shape;
   unsigned int* queue = (unsigned int*)(sl.dev + sl.counters_off + sl.counters_bytes - 256);
   e = jsh_launch_transfer(d_recs, n_req, S->cfg.precision, JSH_SCHED_PERSISTENT, full,
-                          S->cap_pix * (uint64_t)S->cap_nu * (uint64_t)n_req, shape, queue, S->ctx->num_sms, st);
+                          S->cap_pix * (uint64_t)S->cap_nu * (uint64_t)n_req, S->cap_pix, shape, queue,
+                          S->ctx->num_sms, st);
   if (e != cudaSuccess) return e;
   return cudaMemcpyAsync(sl.h_counters, sl.dev + sl.counters_off, sizeof(unsigned long long) * 8 * JSH_MAX_BATCH,
                          cudaMemcpyDeviceToHost, st);
