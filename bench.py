@@ -251,22 +251,26 @@ def gridded_leg(ctx, steps=3):
     t1 = time.perf_counter()
     gid = ctx.grid_upload(xy, vals, tri)
     t2 = time.perf_counter()
-    jet, plane, nu, _ = W.simulation_c3(gid)
     out = {"grid_points": int(xy.shape[0]), "triangles": int(tri.shape[0]), "triangulate_s": t1 - t0,
-           "upload_s": t2 - t1, "image": list(plane.image_size), "n_freq": int(nu.size),
-           "l2": "not flushed: the 13 MB grid is meant to stay resident in the 129 MB L2"}
-    for name, kw in (("batched", dict(precision="mixed", schedule="persistent")),
-                     ("plain_fp64", dict(precision="fp64", schedule="static"))):
+           "upload_s": t2 - t1, "l2": "not flushed: the 13 MB grid is meant to stay resident in the 129 MB L2"}
+    # the batched form on the full 512x512 render (launch shape of the
+    # headline's autotuning), the plain FP64 form on a 128x128 render of the
+    # same region (its grid lookups are FP64, 1/64 rate)
+    for name, kw, scale, reps in (("batched", dict(precision="mixed", schedule="persistent"), 1, steps),
+                                  ("plain_fp64", dict(precision="fp64", schedule="static"), 4, 1)):
+        jet, plane, nu, _ = W.simulation_c3(gid, scale=scale)
         p = J.make_params(**kw, **W.ACCURATE_KW)
-        if name == "batched":
-            ctx.autotune(jet.desc(), plane.desc(), nu, p)
         ms = []
-        for i in range(1 + (steps if name == "batched" else 1)):
+        for i in range(1 + reps):
             _, st = ctx.render(jet.desc(), plane.desc(), nu, p)
             if i > 0:
                 ms.append(st["device_ms"])
+            if st["device_ms"] > 20000:  # a bound on the bench's run time
+                ms.append(st["device_ms"])
+                break
         out[name] = {"rays_per_s": st["n_work_items"] / (np.mean(ms) * 1e-3), "ms": float(np.mean(ms)),
-                     "work_items": int(st["n_work_items"]), "rhs_evals": int(st["rhs_evals"])}
+                     "image": list(plane.image_size), "work_items": int(st["n_work_items"]),
+                     "rhs_evals": int(st["rhs_evals"])}
     return out
 
 

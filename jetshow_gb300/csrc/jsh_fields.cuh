@@ -32,11 +32,11 @@ __device__ __forceinline__ D3 cross(D3 a, D3 b) {
 __device__ inline double grid_value(const JshGrid& G, int field, double px, double py, double nan_value) {
   if (G.n_tri == 0) return nan_value;
   if (!(px >= G.x0 && py >= G.y0)) return nan_value;
-  int i = (int)floor((px - G.x0) / G.hx), j = (int)floor((py - G.y0) / G.hy);
-  if (i >= G.nb) i = G.nb - 1;
-  if (j >= G.nb) j = G.nb - 1;
+  int i = (int)floor((px - G.x0) / G.h), j = (int)floor((py - G.y0) / G.h);
+  if (i >= G.nbx) i = G.nbx - 1;
+  if (j >= G.nby) j = G.nby - 1;
   if (i < 0 || j < 0) return nan_value;
-  int b = j * G.nb + i;
+  int b = j * G.nbx + i;
   int q0 = G.bstart[b], q1 = G.bstart[b + 1];
   for (int q = q0; q < q1; ++q) {
     int t = G.bitems[q];

@@ -38,10 +38,53 @@ __device__ __forceinline__ F3 fcross(F3 a, F3 b) {
 // non-integer exponent, 0 -> +inf / 0 as pow.
 __device__ __forceinline__ float fpow(float x, float e) { return exp2f(e * __log2f(x)); }
 
-// (z, r) in pc on the FP64 bucket grid
+// Point location on a gridded field in FP32: the containing triangle of
+// (z, r) [pc] among the few of its bucket, with barycentric weights (a point
+// within 1e-6 of an edge is accepted by either neighbour: the interpolant is
+// continuous there).  ok = false outside the hull.
+struct GridW {
+  int v0, v1, v2;
+  float w0, w1, w2;
+  bool ok;
+};
+__device__ inline GridW grid_locate32(const JshGrid& G, float px, float py) {
+  GridW g;
+  g.ok = false;
+  if (G.n_tri == 0) return g;
+  const float fx = (px - G.x0f) * G.inv_hf, fy = (py - G.y0f) * G.inv_hf;
+  if (!(fx >= 0.f && fy >= 0.f)) return g;
+  const int i = min((int)fx, G.nbx - 1), j = min((int)fy, G.nby - 1);
+  const int b = j * G.nbx + i;
+  const int q1 = G.bstart[b + 1];
+  for (int q = G.bstart[b]; q < q1; ++q) {
+    const int t = G.bitems[q];
+    const int v0 = G.tri[3 * t], v1 = G.tri[3 * t + 1], v2 = G.tri[3 * t + 2];
+    const float2 a = *reinterpret_cast<const float2*>(G.xyf + 2 * v0);
+    const float2 bb = *reinterpret_cast<const float2*>(G.xyf + 2 * v1);
+    const float2 c = *reinterpret_cast<const float2*>(G.xyf + 2 * v2);
+    const float area = (bb.x - a.x) * (c.y - a.y) - (bb.y - a.y) * (c.x - a.x);
+    if (area == 0.f) continue;
+    const float ia = 1.f / area;
+    const float w0 = ((bb.x - px) * (c.y - py) - (bb.y - py) * (c.x - px)) * ia;
+    const float w1 = ((px - a.x) * (c.y - a.y) - (py - a.y) * (c.x - a.x)) * ia;
+    const float w2 = 1.f - w0 - w1;
+    if (w0 >= -1e-6f && w1 >= -1e-6f && w2 >= -1e-6f) {
+      g = GridW{v0, v1, v2, w0, w1, w2, true};
+      return g;
+    }
+  }
+  return g;
+}
+__device__ __forceinline__ float grid_val32(const JshGrid& G, const GridW& g, int field, float nan_value) {
+  if (!g.ok) return nan_value;
+  const int64_t nf = G.n_fields;
+  const float v = g.w0 * G.val[g.v0 * nf + field] + g.w1 * G.val[g.v1 * nf + field] +
+                  g.w2 * G.val[g.v2 * nf + field];
+  return isnan(v) ? nan_value : v;
+}
+// (z, r) in pc: one field of a gridded field
 __device__ inline float sim32(const JshGrid& G, int field, F3 p, float nan_value) {
-  double r = sqrt((double)p.x * p.x + (double)p.y * p.y);
-  return (float)grid_value(G, field, (double)p.z, r, nan_value);
+  return grid_val32(G, grid_locate32(G, p.z, sqrtf(p.x * p.x + p.y * p.y)), field, nan_value);
 }
 
 // ---------------------------------------------------------------- V
@@ -300,6 +343,20 @@ __device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqCons
     }
     const float bt = b * X.sin_pitch;
     B = f3(bt * px, bt * py, b * X.cos_pitch);
+  } else if (X.sim_shared) {
+    // every field from one grid (the simulation workload): one point location
+    // for Gamma, n, B_p and B_phi
+    const GridW g = grid_locate32(m.grids[0], p.z, sqrtf(p.x * p.x + p.y * p.y));
+    gamma = grid_val32(m.grids[0], g, m.f_v, 1.0f);
+    vdir = f3(0, 0, 1);
+    kinematics32(gamma, vdir, f3(X.nl[0], X.nl[1], X.nl[2]), D, nlp, beta);
+    const float n = grid_val32(m.grids[0], g, m.f_n, 0.f);
+    np_ = m.n_plasma ? n : n / gamma;
+    float s, cph;
+    sincos_atan(p.y / p.x, s, cph);
+    const float bp = grid_val32(m.grids[0], g, m.fb_p, 0.f);
+    const float bphi = grid_val32(m.grids[0], g, m.fb_phi, 0.f);
+    B = f3(-s * bphi, cph * bphi, bp);
   } else {
     if (X.v_const) {
       D = X.D;

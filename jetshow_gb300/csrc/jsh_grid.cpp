@@ -387,14 +387,15 @@ extern "C" int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n, const 
     jsh_set_error("grid points must be finite");
     return JSH_ERR_INVALID;
   }
-  // uniform buckets, about two triangles per bucket; a triangle is listed in
-  // every bucket its bounding box (grown by one bucket) touches
-  int32_t nb = (int32_t)std::ceil(std::sqrt((double)n_tri / 2.0));
-  if (nb < 1) nb = 1;
-  double hx = (x1 - x0) / nb, hy = (y1 - y0) / nb;
-  if (!(hx > 0)) hx = 1;
-  if (!(hy > 0)) hy = 1;
-  const int64_t nbk = (int64_t)nb * nb;
+  // square buckets, about two triangles per bucket; a triangle is listed in
+  // every bucket its bounding box touches, the box grown by 1e-4 of a bucket
+  // so that FP32 lookups near a bucket edge still find it
+  const double ex = x1 - x0, ey = y1 - y0;
+  double h = std::sqrt(std::max(ex * ey, 1e-300) / std::max(1.0, (double)n_tri / 2.0));
+  if (!(h > 0) || !std::isfinite(h)) h = std::max(std::max(ex, ey), 1.0);
+  h = std::max(h, std::max(ex, ey) / 65536.0);  // at most 65536 buckets per side
+  const int32_t nbx = std::max(1, (int32_t)std::ceil(ex / h)), nby = std::max(1, (int32_t)std::ceil(ey / h));
+  const int64_t nbk = (int64_t)nbx * nby;
   std::vector<int32_t> bstart((size_t)nbk + 1, 0);
   std::vector<int32_t> box((size_t)n_tri * 4);
   for (int64_t t = 0; t < n_tri; ++t) {
@@ -406,21 +407,23 @@ extern "C" int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n, const 
       by0 = std::min(by0, xy[2 * v + 1]);
       by1 = std::max(by1, xy[2 * v + 1]);
     }
-    int32_t i0 = (int32_t)std::floor((bx0 - x0) / hx) - 1, i1 = (int32_t)std::floor((bx1 - x0) / hx) + 1;
-    int32_t j0 = (int32_t)std::floor((by0 - y0) / hy) - 1, j1 = (int32_t)std::floor((by1 - y0) / hy) + 1;
+    int32_t i0 = (int32_t)std::floor((bx0 - x0) / h - 1e-4), i1 = (int32_t)std::floor((bx1 - x0) / h + 1e-4);
+    int32_t j0 = (int32_t)std::floor((by0 - y0) / h - 1e-4), j1 = (int32_t)std::floor((by1 - y0) / h + 1e-4);
     i0 = std::max(i0, 0);
     j0 = std::max(j0, 0);
-    i1 = std::min(i1, nb - 1);
-    j1 = std::min(j1, nb - 1);
+    i1 = std::min(i1, nbx - 1);
+    j1 = std::min(j1, nby - 1);
     box[4 * t] = i0, box[4 * t + 1] = i1, box[4 * t + 2] = j0, box[4 * t + 3] = j1;
     for (int32_t j = j0; j <= j1; ++j)
-      for (int32_t i = i0; i <= i1; ++i) bstart[(size_t)j * nb + i + 1]++;
+      for (int32_t i = i0; i <= i1; ++i) bstart[(size_t)j * nbx + i + 1]++;
   }
   for (int64_t b = 0; b < nbk; ++b) bstart[b + 1] += bstart[b];
   std::vector<int32_t> fill(bstart.begin(), bstart.end() - 1), items((size_t)bstart[nbk]);
   for (int64_t t = 0; t < n_tri; ++t)
     for (int32_t j = box[4 * t + 2]; j <= box[4 * t + 3]; ++j)
-      for (int32_t i = box[4 * t]; i <= box[4 * t + 1]; ++i) items[fill[(size_t)j * nb + i]++] = (int32_t)t;
+      for (int32_t i = box[4 * t]; i <= box[4 * t + 1]; ++i) items[fill[(size_t)j * nbx + i]++] = (int32_t)t;
+  std::vector<float> xyf((size_t)2 * n);
+  for (int64_t i = 0; i < 2 * n; ++i) xyf[i] = (float)xy[i];
 
   std::lock_guard<std::mutex> lk(ctx->mu);
   int id = -1;
@@ -431,7 +434,7 @@ extern "C" int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n, const 
     return JSH_ERR_INVALID;
   }
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
-  const size_t o_xy = 0, o_val = o_xy + al(sizeof(double) * 2 * n),
+  const size_t o_xy = 0, o_xyf = o_xy + al(sizeof(double) * 2 * n), o_val = o_xyf + al(sizeof(float) * 2 * n),
                o_tri = o_val + al(sizeof(float) * (size_t)n * n_fields), o_bs = o_tri + al(sizeof(int32_t) * 3 * n_tri),
                o_bi = o_bs + al(sizeof(int32_t) * (nbk + 1)), total = o_bi + al(sizeof(int32_t) * items.size());
   JSH_CUDA_TRY(cudaSetDevice(ctx->device));
@@ -440,6 +443,7 @@ extern "C" int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n, const 
   if (st) return st;
   char* base = (char*)mem;
   cudaError_t e = cudaMemcpy(base + o_xy, xy, sizeof(double) * 2 * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(base + o_xyf, xyf.data(), sizeof(float) * 2 * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(base + o_val, values, sizeof(float) * (size_t)n * n_fields, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(base + o_tri, tri, sizeof(int32_t) * 3 * n_tri, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(base + o_bs, bstart.data(), sizeof(int32_t) * (nbk + 1), cudaMemcpyHostToDevice);
@@ -456,6 +460,7 @@ extern "C" int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n, const 
   S.bytes = total;
   JshGrid& G = S.view;
   G.xy = (const double*)(base + o_xy);
+  G.xyf = (const float*)(base + o_xyf);
   G.val = (const float*)(base + o_val);
   G.tri = (const int32_t*)(base + o_tri);
   G.bstart = (const int32_t*)(base + o_bs);
@@ -463,11 +468,14 @@ extern "C" int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n, const 
   G.n = n;
   G.n_tri = n_tri;
   G.n_fields = n_fields;
-  G.nb = nb;
+  G.nbx = nbx;
+  G.nby = nby;
   G.x0 = x0;
   G.y0 = y0;
-  G.hx = hx;
-  G.hy = hy;
+  G.h = h;
+  G.x0f = (float)x0;
+  G.y0f = (float)y0;
+  G.inv_hf = (float)(1.0 / h);
   *grid_id = id;
   return JSH_OK;
 }

@@ -30,13 +30,15 @@ struct JshCone {
 
 struct JshGrid {         // device view of an uploaded triangulated (z, r) grid
   const double* xy;      // [n][2] (z, r) in pc
+  const float* xyf;      // [n][2] the same in FP32 (mixed-precision lookups)
   const float* val;      // [n][n_fields]
   const int32_t* tri;    // [n_tri][3]
-  const int32_t* bstart; // [nb*nb + 1] bucket -> triangle list offsets
+  const int32_t* bstart; // [nbx*nby + 1] bucket -> triangle list offsets
   const int32_t* bitems; // triangle ids
   int64_t n, n_tri;
-  int32_t n_fields, nb;
-  double x0, y0, hx, hy; // bucket grid origin and cell size
+  int32_t n_fields, nbx, nby, pad_;
+  double x0, y0, h;      // bucket grid origin and (square) cell size
+  float x0f, y0f, inv_hf;
 };
 
 struct JshModel {

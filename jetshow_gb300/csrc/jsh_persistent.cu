@@ -818,6 +818,10 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   X.rtol = (float)req->P.rtol;
   X.kq = (float)m.kq_ratio;
   X.eq = (float)m.eq_ratio;
+  X.sim_shared = (m.v_kind == JSH_V_SIMULATION && m.n_kind == JSH_N_SIMULATION && m.b_kind == JSH_B_SIMULATION &&
+                  m.grid_v == m.grid_b && m.grid_n == m.grid_b)
+                     ? 1
+                     : 0;
   for (int i = 0; i < 8; ++i) {
     X.vq[i] = (float)m.vp[i];
     X.vq_pc[i] = (float)(m.vp[i] / JSH_PC);

@@ -38,6 +38,7 @@ struct JshFreqConst {
 struct JshMixed {
   int32_t v_const;       // ConstFlat velocity: Doppler factor and aberrated LOS are constants
   int32_t helical_bk;    // ConstFlat V, helical conical B, BK n: the fused field path
+  int32_t sim_shared;    // V, N and B all from one grid: one point location per evaluation
   float D, gamma, beta;  // of the constant velocity
   float nlp[3];          // aberrated LOS of the constant velocity
   float nl[3];           // LOS towards the observer (-ray direction)
