@@ -413,7 +413,9 @@ def main():
                         "ms_per_step": float(np.mean(e2e_ms))},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
                 "gridded": gridded,
-                "gpu_launches": 4, "autotuned_shape": tuning, "rhs_evals_per_step": st_b["rhs_evals"],
+                "gpu_launches": int(st_b["kernels_launched"]) * args.steps,
+                "gpu_launches_per_step": {"plane": 2, "hit": 1, "rank": 3, "transfer": 1},
+                "autotuned_shape": tuning, "rhs_evals_per_step": st_b["rhs_evals"],
                 "steps_accepted": st_b["steps_accepted"], "steps_rejected": st_b["steps_rejected"]}
         print(json.dumps(line), flush=True)
     if world > 1:

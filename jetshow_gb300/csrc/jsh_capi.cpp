@@ -337,6 +337,8 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
                                    ctx->num_sms, stream));
   JSH_CUDA_TRY(cudaEventRecord(ctx->ws_ready, stream));
   ctx->last_pending = true;
+  // plane (2), hit, transfer; the persistent mixed schedule adds 3 ranking kernels
+  ctx->last_kernels = (params->precision == JSH_PREC_MIXED && params->schedule == JSH_SCHED_PERSISTENT) ? 7 : 4;
   ctx->last_counters_off = L.off_counters;
   ctx->last_nhit_off = L.off_nhit;
   ctx->last_npix = npix;
@@ -365,7 +367,7 @@ int collect_stats(jsh_ctx* ctx, jsh_stats* s) {
   st.steps_accepted = c[1];
   st.steps_rejected = c[2];
   st.status_or = (uint32_t)c[3];
-  st.kernels_launched = 4;
+  st.kernels_launched = ctx->last_kernels;
   ctx->last = st;
   ctx->last_pending = false;
   *s = st;

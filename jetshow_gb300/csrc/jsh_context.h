@@ -55,6 +55,7 @@ struct jsh_ctx {
   size_t last_counters_off = 0, last_nhit_off = 0;
   uint64_t last_npix = 0;
   int last_n_nu = 0;
+  int last_kernels = 0;
 };
 
 // Helpers shared by the C-ABI translation units.
