@@ -195,10 +195,10 @@ typedef struct jsh_params {
 } jsh_params;
 
 /* Mixed precision: start the IQUV pass of an optically thick ray where the
- * optical depth from the observer first exceeds tau_thick = 20 / (1 - p)
+ * optical depth from the observer first exceeds tau_thick = 16 / (1 - p)
  * (p = k_Q / k_I + 0.05, at most 0.95; p = 0 for I-only output) instead of
  * at tau_max.  The Stokes vector entering at that depth reaches the observer
- * attenuated by at least exp(-20) ~ 2e-9 (500 times below the relative
+ * attenuated by at least exp(-16) ~ 1.1e-7 (10 times below the relative
  * tolerance 1e-6 of the integration itself), so the image agrees with the
  * integration from tau_max to that factor; thick rays need a small fraction
  * of the stiff IQUV steps.  This flag turns it off (integrate from tau_max

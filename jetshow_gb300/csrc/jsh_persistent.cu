@@ -843,10 +843,10 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   // optically thick start of the IQUV pass: the Stokes vector decays at
   // least at rate k_I (1 - |(k_Q, k_U, k_V)| / k_I) along the ray (the
   // symmetric part of the transfer matrix; Faraday terms only rotate), so
-  // what enters at optical depth tau_thick is attenuated by exp(-20)
+  // what enters at optical depth tau_thick is attenuated by exp(-16)
   {
     double p = req->P.full ? std::min(0.95, m.kq_ratio + 0.05) : 0.0;
-    double thick = 20.0 / (1.0 - p);
+    double thick = 16.0 / (1.0 - p);
     X.tau_thick = (req->P.flags & JSH_FLAG_IQUV_FROM_TAU_MAX) || !(thick < req->P.tau_max) ? INFINITY : thick;
   }
   if (m.v_kind == JSH_V_CONST_FLAT) {

@@ -7,9 +7,9 @@
  * contract the GPU geometry kernels are bit-exact against.
  *
  * Parity is pinned by the reference's Cone::hit golden cases
- * (tests/simple_test.cpp:17-101) and by analytic known answers; the rest of
- * the transfer path is unpinned because the reference cannot be built here
- * (Boost.odeint, Eigen, CGAL absent).
+ * (tests/simple_test.cpp:17-101) and by analytic known answers; for the rest
+ * of the transfer path parity unpinned: the reference cannot be built here
+ * (Boost.odeint, Eigen, CGAL absent) and holds no golden vectors for it.
  *
  * Third-party arithmetic restated from published sources:
  *  - Dormand & Prince (1980) RK5(4)7M tableau; the continuous extension of
