@@ -481,6 +481,21 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       }
       return;
     }
+    // landing on the optically thick depth: a tau step may not overshoot
+    // tau_thick by more than 25 %, so that the IQUV pass can start at the end
+    // of the crossing step, where tau is as accurate as the integration (near
+    // a jet's core one step can span thousands in tau, and its dense output
+    // is no guide to where tau_thick lies inside it)
+    if (tau && L.first_seg < 0 && L.tau_seg.hi < L.thick_left && L.tau_seg.hi + inc[0] > 1.25f * L.thick_left) {
+      L.dt = h * fmaxf((1.1f * L.thick_left - L.tau_seg.hi) / inc[0], 0.01f);
+      L.last = false;
+      L.rej++;
+      if (++L.fails >= dp::FAIL_LIMIT) {
+        L.status |= JSH_ST_FAIL_LIMIT;
+        goto abort;
+      }
+      return;
+    }
     // accept
     const DF t_prev = L.t;
     const DF t_new = L.last ? L.length : df_add(L.t, h);
@@ -506,16 +521,11 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       const DF tau_prev = L.tau_seg;
       L.tau_seg = df_add(L.tau_seg, inc[0]);
       if (L.first_seg < 0 && L.tau_seg.hi >= L.thick_left) {
-        // optically thick from here on: the IQUV pass starts where the
-        // optical depth reaches tau_thick on this step's dense output (to
-        // within 1; a step can span thousands in tau near a jet's core), or
-        // at the step's start if the bisection does not settle; the tau
-        // pass goes on for the tau image
-        const double t_old = df_val(t_prev);
-        double tc = crossing_time(df_val(tau_prev), t_old, (double)h, h, K(0, 0), K(2, 0), K(3, 0), K(4, 0),
-                                  K(5, 0), K(6, 0), inc[0], R.mix.tau_thick - L.tau_bg, 1.0);
+        // optically thick from here on (tau within [1, 1.25] tau_thick): the
+        // IQUV pass starts at the end of this step; the tau pass goes on for
+        // the tau image
         L.first_seg = L.seg;
-        L.t_first = tc < 0.0 ? t_old : tc;
+        L.t_first = df_val(t_new);
       }
       if (L.tau_seg.hi > R.mix.tau_max_hi || (L.tau_seg.hi == R.mix.tau_max_hi && L.tau_seg.lo >= R.mix.tau_max_lo)) {
         L.status |= JSH_ST_TAU_CROSSED;
