@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=int, default=1, help="shrink the image (debug only)")
+    ap.add_argument("--workload", default="conical", choices=["conical", "simulation-grid"],
+                    help="the rendered jet (simulation-grid: profiling of the gridded path only)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-gridded", dest="gridded", action="store_false",
                     help="skip the simulation-grid leg")
@@ -109,8 +111,16 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def workload(scale):
+def workload(scale, name="conical", ctx=None):
+    """The headline workload (the conical jet on the 512x1024 log plane), or
+    the simulation-grid jet (its grid triangulated and uploaded to ctx) for
+    profiling that path."""
     from jetshow_gb300 import workloads as W
+    if name == "simulation-grid":
+        from jetshow_gb300.runtime import triangulate
+        xy, vals = W.simulation_grid_c3()
+        gid = ctx.grid_upload(xy, vals, triangulate(xy))
+        return W.simulation_c3(gid, scale=scale)
     return W.conical_c1(scale=scale)
 
 
@@ -290,7 +300,7 @@ def main():
     from jetshow_gb300.runtime import Context
 
     ctx = Context(local)
-    jet, plane, nu, kw = workload(args.scale)
+    jet, plane, nu, kw = workload(args.scale, args.workload, ctx)
     model, pdesc = jet.desc(), plane.desc()
     na, nl = plane.image_size
     npix = na * nl
@@ -354,7 +364,8 @@ def main():
         ms_p, st_p = timed(p_plain, 1, 1)
         plain_rate = st_p["n_work_items"] / (np.mean(ms_p) * 1e-3)
         out_p = {k: v.cpu().numpy() for k, v in planes.items()}
-    rel = errors_vs_converged(jet, plane, nu, {"batched": out_b, "plain": out_p}) if rank == 0 else {}
+    conical = args.workload == "conical"
+    rel = errors_vs_converged(jet, plane, nu, {"batched": out_b, "plain": out_p}) if rank == 0 and conical else {}
 
     # ---- end to end through the C ABI with pinned host buffers
     host = {k: torch.empty((nu.size, npix), dtype=torch.float64, pin_memory=True) for k in
@@ -391,7 +402,7 @@ def main():
             "mufu": {"achieved_tops": evals_per_s * CENSUS_MUFU / 1e12, "peak_tops": peaks["mufu_tops"],
                      "frac": evals_per_s * CENSUS_MUFU / 1e12 / peaks["mufu_tops"]},
             "fp64_peak_tflops": peaks["fp64_tflops"]}
-    cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 else None
+    cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 and conical else None
     serving = serving_leg(ctx, args.serve_requests) if args.serve_requests > 0 else None
     gridded = gridded_leg(ctx) if args.gridded else None
 
