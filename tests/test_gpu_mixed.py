@@ -13,6 +13,7 @@ percent (for the FP64 reference too); the converged oracle is the arbiter.
 import numpy as np
 import pytest
 
+from jetshow_gb300 import _capi as A
 from jetshow_gb300 import jet as J
 from jetshow_gb300 import workloads as W
 from helpers import compare_images, flat
@@ -85,3 +86,36 @@ def test_persistent_refill_thresholds_agree(ctx, refill):
     # the same per-item arithmetic whichever lane or warp runs an item
     for k in ("tau", "I", "Q", "U", "V", "status"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_optically_thick_start_matches_integration_from_tau_max(ctx):
+    # the IQUV pass started at tau_thick agrees with the reference's start at
+    # tau_max to the integration's own accuracy (the truncated part is
+    # attenuated by at least exp(-16))
+    jet, plane, nu, _ = W.conical_c1(scale=16)
+    kw = dict(W.ACCURATE_KW)
+    a, sa = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent", **kw))
+    b, sb = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent",
+                                                                   flags=A.FLAG_IQUV_FROM_TAU_MAX, **kw))
+    assert sa["rhs_evals"] < sb["rhs_evals"]
+    assert np.array_equal(a["status"] & 1, b["status"] & 1)
+    # the tau pass differs only by the steps that land on tau_thick
+    both = (a["tau"] < 1e4) & (b["tau"] < 1e4) & ((b["status"] & 1) != 0)
+    assert np.max(np.abs(a["tau"][both] - b["tau"][both]) / np.abs(b["tau"][both])) < 1e-5
+    for f in range(nu.size):
+        imax = np.abs(b["I"][f]).max()
+        sel = np.abs(b["I"][f]) > 1e-6 * imax
+        assert np.max(np.abs(a["I"][f][sel] - b["I"][f][sel]) / np.abs(b["I"][f][sel])) < 2e-5
+        for k in ("Q", "U", "V"):
+            assert np.max(np.abs(a[k][f] - b[k][f])) < 2e-5 * imax
+
+
+def test_cost_map_counts_every_evaluation(ctx):
+    jet, plane, nu, _ = W.conical_c0(scale=8)
+    for prec, sched in (("mixed", "persistent"), ("fp64", "static")):
+        g, st = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision=prec, schedule=sched,
+                                                                       flags=A.FLAG_COST_MAP, **W.ACCURATE_KW))
+        hit = (g["status"] & 1) != 0
+        assert np.all(g["l"][hit] > 0) and np.all(g["l"][~hit] == 0)
+        assert np.all(g["l"] == np.round(g["l"]))
+        assert int(g["l"].sum()) == st["rhs_evals"]
