@@ -460,10 +460,11 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       // (e_Q - k_Q I, ...) and the rounding noise of their error estimate
       // reaches ~0.7 of the floor, which pins the estimate in odeint's
       // no-growth band [0.5, 1] (95 % of the core rays' steps were there); a
-      // 3x floor cuts their evaluations by 16 %.  Optically thin steps keep
-      // the 1x floor (their Q/U control is what keeps far rays from stepping
-      // over the narrow dip of B_perp where they pass the jet axis).
-      const float fl_pol = (adt * fabsf(L.kI1) > 0.01f) ? 3.f * floor_ : floor_;
+      // 10x floor cuts their evaluations by 34 % (errors unchanged: the
+      // allowed error per step is still 10 u h scale).  Optically thin steps
+      // keep the 1x floor (their Q/U control is what keeps far rays from
+      // stepping over the narrow dip of B_perp where they pass the jet axis).
+      const float fl_pol = (adt * fabsf(L.kI1) > 0.01f) ? 10.f * floor_ : floor_;
 #pragma unroll
       for (int c = 0; c < NX; ++c) {
         const float fl = (c == 0) ? floor_ : fl_pol;
