@@ -48,12 +48,15 @@ CENSUS_MUFU = 14
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=int, default=1, help="shrink the image (debug only)")
     ap.add_argument("--workload", default="conical", choices=["conical", "simulation-grid"],
                     help="the rendered jet (simulation-grid: profiling of the gridded path only)")
+    ap.add_argument("--shape", default="",
+                    help="block,ctas_per_sm,refill,compact: fixed launch shape instead of the autotuner "
+                         "(profiling: the first persistent launch is then a warm-up step)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-gridded", dest="gridded", action="store_false",
                     help="skip the simulation-grid leg")
@@ -81,7 +84,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -341,7 +344,14 @@ def main():
 
     # ---- batched form (headline): the launch shape autotuned on this
     # request (untimed), then clocks sampled during the timed steps
-    tuning = ctx.autotune(model, pdesc, nu, p_batched)
+    if args.shape:
+        b, c, r, k = (int(x) for x in args.shape.split(","))
+        p_batched = J.make_params(precision="mixed", schedule="persistent", block_size=b, ctas_per_sm=c,
+                                  refill_threshold=r, flags=A.FLAG_COMPACT_REGS if k else 0, **kw)
+        tuning = {"block_size": b, "ctas_per_sm": c, "refill_threshold": r, "compact": k, "ms": None,
+                  "fixed": True}
+    else:
+        tuning = ctx.autotune(model, pdesc, nu, p_batched)
     barrier()
     with ClockSampler(local) as clk:
         ms_b, st_b = timed(p_batched, args.steps, args.warmup)

@@ -118,6 +118,20 @@ class ParabaloidCone : public BaseGeometry {
   }
 };
 
+// SimulationGeometry(tree) (include/Geometry.h:58-65, src/Geometry.cpp:92-132):
+// the reference passes an AABB tree over CGAL::convex_hull_3 of the grid
+// points revolved at 36 azimuths (src/main.cpp:880-897); here the hull is
+// built from the (z, r) points [pc] and uploaded by this constructor.
+class SimulationGeometry : public BaseGeometry {
+ public:
+  SimulationGeometry(const std::vector<double>& zr, int n_circle = 36, jsh_ctx* ctx = default_context())
+      : BaseGeometry(JSH_GEO_SIMULATION, Vector3d(), Vector3d(0, 0, 1)) {
+    int32_t id = 0;
+    check(jsh_hull_upload(ctx, zr.data(), (int64_t)(zr.size() / 2), n_circle, &id));
+    d_.hull_id = id;
+  }
+};
+
 // --------------------------------------------------------------- fields
 class Field {
  public:

@@ -27,6 +27,10 @@
  *       src/SimulationInterpolater.cpp:30-117      -> jsh_grid_triangulate,
  *                                                      jsh_grid_upload,
  *                                                      jsh_grid_interpolate
+ *   - SimulationGeometry + its hull (convex_hull_3 of the revolved grid
+ *     points, AABB tree of the faces)
+ *       src/Geometry.cpp:92-132, src/main.cpp:880-897 -> jsh_hull_upload,
+ *                                                      JSH_GEO_SIMULATION
  *   - comoving_transfer_distance2 / mas_to_pc
  *       src/utils.cpp:186-208                       -> jsh_mas_to_pc
  *
@@ -73,12 +77,15 @@ enum jsh_geometry_kind {
   JSH_GEO_CONE = 1,            /* Cone(origin, direction, angle, big_scale)        */
   JSH_GEO_CYLINDER = 2,        /* Cylinder(origin, direction, r)                   */
   JSH_GEO_PARABALOID = 3,      /* Parabaloid(origin, direction, r0, big_scale)     */
-  JSH_GEO_PARABALOID_CONE = 4  /* ParabaloidCone(origin, direction, r0, z0, scale) */
+  JSH_GEO_PARABALOID_CONE = 4, /* ParabaloidCone(origin, direction, r0, z0, scale) */
+  JSH_GEO_SIMULATION = 5       /* SimulationGeometry(tree): the convex hull of a
+                                  revolved (z, r) point set, hull_id from
+                                  jsh_hull_upload; other fields unused       */
 };
 
 typedef struct jsh_geometry_desc {
   int32_t kind;        /* enum jsh_geometry_kind */
-  int32_t reserved;
+  int32_t hull_id;     /* JSH_GEO_SIMULATION: id from jsh_hull_upload (else 0) */
   double origin[3];    /* [cm] */
   double direction[3]; /* normalised by the library, as the constructors do */
   double angle;        /* cone half-opening angle [rad] */
@@ -208,6 +215,11 @@ typedef struct jsh_params {
 /* Cost map: the l plane receives each item's number of right-hand-side
  * evaluations instead of the path length (schedule and cost studies). */
 #define JSH_FLAG_COST_MAP 0x2
+/* Mixed persistent schedule: launch the register-capped build of the
+ * transfer kernel (at most 128 threads per CTA; more resident warps per SM).
+ * Results are bitwise those of the default build; jsh_autotune chooses
+ * between the two for requests that leave the launch knobs at 0. */
+#define JSH_FLAG_COMPACT_REGS 0x4
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,
@@ -341,6 +353,23 @@ int jsh_grid_interpolate(jsh_ctx* ctx, int32_t grid_id, int32_t field,
                          const double* zr, int64_t n, double nan_value,
                          double* out);
 
+/* --------------------------------------------------- simulation geometry */
+/* The jet boundary of a gridded simulation (SimulationGeometry,
+ * src/Geometry.cpp:92-132): the convex hull of the (z, r) points zr[n][2]
+ * (pc) revolved about the z axis at n_circle azimuths phi_j = 2 pi j /
+ * n_circle, the point (r sin phi_j, r cos phi_j, z) (the reference builds it
+ * with n_circle = 36, src/main.cpp:880-897).  That hull is the set of points
+ * whose n_circle-gon "radius" about the axis is at most R(z), R the upper
+ * envelope of the convex hull of the (z, r) profile, so only the profile is
+ * stored (host-built once, a few KB on the device).  A ray's segment is the
+ * whole line's intersection with the hull (the reference intersects the
+ * line, not the half-line), point_in at the smaller ray parameter.  Requires
+ * r >= 0, n >= 2 and two distinct z values; 3 <= n_circle <= 4096.  Returns a
+ * hull id for jsh_geometry_desc.hull_id (kind JSH_GEO_SIMULATION). */
+#define JSH_MAX_HULLS 16
+int jsh_hull_upload(jsh_ctx* ctx, const double* zr, int64_t n, int32_t n_circle,
+                    int32_t* hull_id);
+
 /* --------------------------------------------------------- serving */
 typedef struct jsh_server jsh_server;
 typedef uint64_t jsh_request_id;
@@ -385,13 +414,14 @@ typedef struct jsh_tuning {
   int32_t block_size;
   int32_t ctas_per_sm;
   int32_t refill_threshold;
-  int32_t reserved;
+  int32_t compact;      /* 1: the register-capped build (JSH_FLAG_COMPACT_REGS) */
   double ms;            /* best measured time */
 } jsh_tuning;
 
-/* Time the persistent schedule over a grid of block sizes, CTAs per SM and
- * refill thresholds on this request and store the fastest in the context;
- * later requests with block_size == 0 use it. */
+/* Time the persistent schedule over a grid of kernel builds (default and
+ * register-capped), block sizes, CTAs per SM and refill thresholds on this
+ * request and store the fastest in the context; later requests with
+ * block_size == 0 use it. */
 int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model,
                  const jsh_plane_desc* plane, const double* nu_hz,
                  int32_t n_nu, const jsh_params* params, jsh_tuning* best);

@@ -31,9 +31,10 @@ ST_DT_UNDERFLOW = 0x80
 ST_IQUV = 0x100
 FLAG_IQUV_FROM_TAU_MAX = 0x1
 FLAG_COST_MAP = 0x2
+FLAG_COMPACT_REGS = 0x4
 ST_ERRORS = ST_STEP_LIMIT | ST_FAIL_LIMIT | ST_BISECT_LIMIT | ST_NAN | ST_DT_UNDERFLOW
 
-GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE = 1, 2, 3, 4
+GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE, GEO_SIMULATION = 1, 2, 3, 4, 5
 
 B_RANDOM_SCALAR = 1
 B_RANDOM_SCALAR_Z = 2
@@ -77,7 +78,7 @@ SCALAR_B_KINDS = (B_RANDOM_SCALAR, B_RANDOM_SCALAR_Z, B_COMPOSITE_RANDOM_SCALAR_
 class GeometryDesc(C.Structure):
     _fields_ = [
         ("kind", C.c_int32),
-        ("reserved", C.c_int32),
+        ("hull_id", C.c_int32),
         ("origin", C.c_double * 3),
         ("direction", C.c_double * 3),
         ("angle", C.c_double),
@@ -216,7 +217,7 @@ class Tuning(C.Structure):
         ("block_size", C.c_int32),
         ("ctas_per_sm", C.c_int32),
         ("refill_threshold", C.c_int32),
-        ("reserved", C.c_int32),
+        ("compact", C.c_int32),
         ("ms", C.c_double),
     ]
 
@@ -249,6 +250,7 @@ SIGNATURES = [
      [C.c_void_p, _D, C.c_int64, _P(C.c_float), C.c_int32, _P(C.c_int32), C.c_int64, _P(C.c_int32)]),
     ("jsh_grid_interpolate", C.c_int,
      [C.c_void_p, C.c_int32, C.c_int32, _D, C.c_int64, C.c_double, _D]),
+    ("jsh_hull_upload", C.c_int, [C.c_void_p, _D, C.c_int64, C.c_int32, _P(C.c_int32)]),
     ("jsh_server_create", C.c_int, [C.c_void_p, _P(ServerConfig), _P(C.c_void_p)]),
     ("jsh_server_destroy", None, [C.c_void_p]),
     ("jsh_server_submit", C.c_int,

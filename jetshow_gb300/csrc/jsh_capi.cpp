@@ -121,6 +121,7 @@ JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params)
   if (params->block_size > 0) s.block_size = params->block_size;
   if (params->ctas_per_sm > 0) s.ctas_per_sm = params->ctas_per_sm;
   if (params->refill_threshold > 0) s.refill_threshold = params->refill_threshold;
+  if (params->flags & JSH_FLAG_COMPACT_REGS) s.compact = 1;
   if (s.block_size < 32) s.block_size = 32;
   if (s.block_size > 512) s.block_size = 512;
   s.block_size = s.block_size / 32 * 32;
@@ -167,6 +168,8 @@ int jsh_prepare_request(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_pla
     jsh_set_error("s = 2 makes k_C_r singular (2/(s-2), src/utils.cpp:96)");
     return JSH_ERR_INVALID;
   }
+  st = jsh_resolve_hull(ctx, &req->model);
+  if (st) return st;
   // gridded fields
   int gids[3] = {req->model.grid_b, req->model.grid_n, req->model.grid_v};
   for (int k = 0; k < 3; ++k) {
@@ -258,6 +261,8 @@ extern "C" void jsh_ctx_destroy(jsh_ctx* c) {
   if (c->ws) jsh_free_device(c, c->ws, c->ws_cap);
   for (auto& g : c->grids)
     if (g.used) jsh_free_device(c, g.mem, g.bytes);
+  for (auto& h : c->hulls)
+    if (h.used) jsh_free_device(c, h.mem, h.bytes);
   if (c->h_req) cudaFreeHost(c->h_req);
   if (c->h_fc) cudaFreeHost(c->h_fc);
   if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -490,6 +495,8 @@ extern "C" int jsh_trace_plane(jsh_ctx* ctx, const jsh_model_desc* model, const 
   memset(&req, 0, sizeof(req));
   int st = jsh_compile_model(model, &req.model);
   if (st) return st;
+  st = jsh_resolve_hull(ctx, &req.model);
+  if (st) return st;
   st = jsh_compile_plane(plane, &req.plane);
   if (st) return st;
   uint64_t npix = plane->n_across * plane->n_along;
@@ -539,6 +546,8 @@ extern "C" int jsh_hit_rays(jsh_ctx* ctx, const jsh_model_desc* model, const dou
   JSH_CUDA_TRY(cudaSetDevice(ctx->device));
   JshModel m;
   int st = jsh_compile_model(model, &m);
+  if (st) return st;
+  st = jsh_resolve_hull(ctx, &m);
   if (st) return st;
   size_t o_orig = 0, o_dir = align_up(24 * n), o_nseg = align_up(o_dir + 24 * n), o_seg = align_up(o_nseg + 4 * n),
          o_st = align_up(o_seg + 96 * n), total = align_up(o_st + 4 * n);

@@ -26,6 +26,13 @@ struct JshGridSlot {
   size_t bytes = 0;
 };
 
+struct JshHullSlot {
+  bool used = false;
+  JshHull view{};
+  void* mem = nullptr;  // one allocation holding the profile arrays
+  size_t bytes = 0;
+};
+
 // Layout of one request's device memory inside an arena allocation.
 struct JshRequestLayout {
   size_t off_req, off_counters, off_nhit, off_queue, off_buckets, off_nu, off_fc, off_along_size, off_along_center,
@@ -48,8 +55,9 @@ struct jsh_ctx {
   JshFreqConst* h_fc = nullptr;              // pinned staging of its frequency constants [4096]
   unsigned long long* h_counters = nullptr;  // pinned [8]
   JshGridSlot grids[JSH_MAX_GRIDS];
+  JshHullSlot hulls[JSH_MAX_HULLS];
   bool tuned = false;
-  JshLaunchShape shape{128, 0, 8};
+  JshLaunchShape shape{128, 0, 8, 0};
   jsh_stats last{};
   bool last_pending = false;
   size_t last_counters_off = 0, last_nhit_off = 0;
@@ -77,6 +85,10 @@ int ensure_workspace(jsh_ctx* ctx, size_t need);
 int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_desc* plane, const double* nu_hz,
                    int32_t n_nu, const jsh_params* params, cudaStream_t stream, const jsh_image* dev_out,
                    JshRequestLayout* L_out, uint64_t* npix_out);
+// SimulationGeometry: copy the context's view of hull model->hull_id into
+// the compiled model (JSH_ERR_NOT_FOUND for an unknown id); no-op for the
+// analytic geometries.  Called with ctx->mu held.
+int jsh_resolve_hull(jsh_ctx* ctx, JshModel* model);
 // Counters of the last enqueued request (synchronises with it).
 int collect_stats(jsh_ctx* ctx, jsh_stats* s);
 void jsh_set_error(const char* fmt, ...);

@@ -8,6 +8,7 @@
 // Reference: src/Cone.cpp:48-118, src/Geometry.cpp:28-78,
 // src/Cylinder.cpp:29-99, src/Parabaloid.cpp:39-60,
 // src/ParabaloidCone.cpp:36-94, src/Intersection.cpp:41-62,
+// src/Geometry.cpp:92-132 (SimulationGeometry),
 // src/Image.cpp:44-194, src/ImagePlane.cpp:11-33.
 #pragma once
 
@@ -258,6 +259,110 @@ __device__ __forceinline__ void parabaloid_cone_hit(const JshModel& m, V3 ro, V3
   h.s[0] = Seg{pin, pout};
 }
 
+// ------------------------------------------------------- SimulationGeometry
+// Line / revolved-hull intersection (src/Geometry.cpp:97-132: the LINE
+// through the ray, in pc, against the convex hull of the revolved grid
+// points; the two points scaled back to cm).  The hull is the intersection
+// over the n_circle azimuthal sectors k of the slabs {g_k . (x, y) <= R(z),
+// z_min <= z <= z_max} (see jsh_hull.cpp).  Along the line, with z as the
+// parameter (d_z != 0), slab k is the z interval where
+// D(z) = R(z) - (A + B z) >= 0, A + B z the line's g_k coordinate; D is
+// concave and piecewise linear with breaks at the profile vertices, so its
+// sign at the vertices (binary searches) finds the profile edge or the cap
+// that the line crosses on each side, and the crossing parameter comes from
+// that edge's half-plane.  The segment is [max_k t_in, min_k t_out].
+// point_in is the point of smaller t (the reference orders CGAL's two
+// points by the sign of x, which agrees when they straddle x = 0 and is
+// the AABB traversal order otherwise).
+__device__ __forceinline__ double hull_D(const JshHull& H, int i, double A, double B) {
+  return sb(H.vR[i], ad(A, ml(B, H.vz[i])));
+}
+// t where the line crosses the half-plane of edge e (sector coordinates u0 +
+// t u1 of the line); a line parallel to the edge (beta == 0, only through
+// rounding) takes the t of the edge's lower vertex height.
+__device__ __forceinline__ double hull_edge_t(const JshHull& H, int e, double u0, double u1, double oz, double dz) {
+  const double a = H.abc[3 * e], b = H.abc[3 * e + 1], c = H.abc[3 * e + 2];
+  const double alpha = sb(ad(ml(a, u0), ml(b, oz)), c);
+  const double beta = ad(ml(a, u1), ml(b, dz));
+  if (beta == 0.0) return dv(sb(H.vz[e], oz), dz);
+  return dv(-alpha, beta);
+}
+
+static __device__ __noinline__ void simulation_hit(const JshHull& H, V3 ro_cm, V3 rd, Hits& h) {
+  const V3 o = vdiv(ro_cm, JSH_PC);
+  const int m = H.m;
+  double tlo = -INFINITY, thi = INFINITY;
+  if (rd.z == 0.0) {
+    // the line stays at z = o.z: one radius bound R(o.z) for every sector
+    if (!(o.z >= H.z_min && o.z <= H.z_max)) return;
+    int lo = 0, hi = m;  // edge e with vz[e] <= o.z <= vz[e+1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (H.vz[mid] <= o.z) lo = mid;
+      else hi = mid;
+    }
+    const double a = H.abc[3 * lo], b = H.abc[3 * lo + 1], c = H.abc[3 * lo + 2];
+    const double R0 = dv(sb(c, ml(b, o.z)), a);
+    for (int k = 0; k < H.n_circle; ++k) {
+      const double gx = H.g[2 * k], gy = H.g[2 * k + 1];
+      const double u0 = ad(ml(gx, o.x), ml(gy, o.y)), u1 = ad(ml(gx, rd.x), ml(gy, rd.y));
+      if (u1 > 0.0) thi = fmin(thi, dv(sb(R0, u0), u1));
+      else if (u1 < 0.0) tlo = fmax(tlo, dv(sb(R0, u0), u1));
+      else if (u0 > R0) return;
+    }
+  } else {
+    const double t_zmin = dv(sb(H.z_min, o.z), rd.z), t_zmax = dv(sb(H.z_max, o.z), rd.z);
+    for (int k = 0; k < H.n_circle; ++k) {
+      const double gx = H.g[2 * k], gy = H.g[2 * k + 1];
+      const double u0 = ad(ml(gx, o.x), ml(gy, o.y)), u1 = ad(ml(gx, rd.x), ml(gy, rd.y));
+      const double B = dv(u1, rd.z), A = sb(u0, ml(B, o.z));
+      // vertex of D's maximum: the first edge whose slope falls below B
+      int lo = 0, hi = m;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (sb(sb(H.vR[mid + 1], H.vR[mid]), ml(B, sb(H.vz[mid + 1], H.vz[mid]))) < 0.0) hi = mid;
+        else lo = mid + 1;
+      }
+      const int top = lo;
+      if (!(hull_D(H, top, A, B) >= 0.0)) return;  // this sector's slab misses the line
+      double ta, tb;
+      if (hull_D(H, 0, A, B) >= 0.0) {
+        ta = t_zmin;
+      } else {
+        int l = 0, r = top;  // D(l) < 0 <= D(r)
+        while (r - l > 1) {
+          const int mid = (l + r) >> 1;
+          if (hull_D(H, mid, A, B) >= 0.0) r = mid;
+          else l = mid;
+        }
+        ta = hull_edge_t(H, l, u0, u1, o.z, rd.z);
+      }
+      if (hull_D(H, m, A, B) >= 0.0) {
+        tb = t_zmax;
+      } else {
+        int l = top, r = m;  // D(l) >= 0 > D(r)
+        while (r - l > 1) {
+          const int mid = (l + r) >> 1;
+          if (hull_D(H, mid, A, B) >= 0.0) l = mid;
+          else r = mid;
+        }
+        tb = hull_edge_t(H, l, u0, u1, o.z, rd.z);
+      }
+      tlo = fmax(tlo, fmin(ta, tb));
+      thi = fmin(thi, fmax(ta, tb));
+    }
+  }
+  if (!(tlo < thi)) {
+    // tangent (one point): the reference reads a second point that CGAL did
+    // not return
+    if (tlo == thi) h.status |= JSH_ST_UB_GEOMETRY;
+    return;
+  }
+  h.n = 1;
+  h.s[0].in = vmul(ray_point(o, rd, tlo), JSH_PC);
+  h.s[0].out = vmul(ray_point(o, rd, thi), JSH_PC);
+}
+
 __device__ __forceinline__ void geo_hit(const JshModel& m, V3 ro, V3 rd, Hits& h) {
   h.n = 0;
   h.status = 0;
@@ -266,6 +371,7 @@ __device__ __forceinline__ void geo_hit(const JshModel& m, V3 ro, V3 rd, Hits& h
     case JSH_GEO_CYLINDER: cylinder_hit(m, ro, rd, h); break;
     case JSH_GEO_PARABALOID: parabaloid_hit(m.r0, ro, rd, h); break;
     case JSH_GEO_PARABALOID_CONE: parabaloid_cone_hit(m, ro, rd, h); break;
+    case JSH_GEO_SIMULATION: simulation_hit(m.hull, ro, rd, h); break;
     default: break;
   }
 }

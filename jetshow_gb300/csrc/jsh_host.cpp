@@ -91,7 +91,10 @@ int jsh_compile_model(const jsh_model_desc* d, JshModel* m) {
   m->gox = g.origin[0];
   m->goy = g.origin[1];
   m->goz = g.origin[2];
-  Vd dir = normalize(Vd{g.direction[0], g.direction[1], g.direction[2]});
+  // SimulationGeometry has no origin or axis of its own (the hull is
+  // revolved about the z axis); its profile is resolved from the context
+  Vd dir = g.kind == JSH_GEO_SIMULATION ? Vd{0.0, 0.0, 1.0}
+                                        : normalize(Vd{g.direction[0], g.direction[1], g.direction[2]});
   if (!((dir.x * dir.x + dir.y * dir.y) + dir.z * dir.z > 0)) {
     jsh_set_error("geometry direction is zero");
     return JSH_ERR_INVALID;
@@ -131,6 +134,9 @@ int jsh_compile_model(const jsh_model_desc* d, JshModel* m) {
                         cos(atan(0.5 * r0 * pow(z0 * JSH_PC, -0.5))), g.big_scale};
       break;
     }
+    case JSH_GEO_SIMULATION:
+      m->hull_id = g.hull_id;
+      break;
     default:
       jsh_set_error("unknown geometry kind %d", g.kind);
       return JSH_ERR_INVALID;

@@ -13,6 +13,7 @@ struct JshLaunchShape {
   int block_size;        // threads per CTA of the transfer kernel
   int ctas_per_sm;       // persistent schedule: CTAs per SM (0: occupancy max)
   int refill_threshold;  // persistent schedule: refill when >= this many lanes idle
+  int compact;           // mixed persistent schedule: the 168-register build (<= 128 threads)
 };
 
 // Ray generation: along sizes and centres (sequential recurrence of
@@ -46,5 +47,7 @@ cudaError_t jsh_launch_plane_rays(const JshPlane& plane, double* d_orig, double*
 cudaError_t jsh_launch_grid_interp(const JshGrid& grid, int field, const double* d_zr, int64_t n,
                                    double nan_value, double* d_out, cudaStream_t stream);
 
-// Largest resident CTAs per SM of the persistent transfer kernel.
-int jsh_persistent_occupancy(int precision, bool full, int block_size);
+// Largest resident CTAs per SM of the persistent transfer kernel (compact:
+// the register-capped build of the mixed kernel; 0 if it cannot run
+// block_size threads).
+int jsh_persistent_occupancy(int precision, bool full, int block_size, bool compact = false);

@@ -41,6 +41,22 @@ struct JshGrid {         // device view of an uploaded triangulated (z, r) grid
   float x0f, y0f, inv_hf;
 };
 
+// Device view of an uploaded simulation hull (SimulationGeometry): the
+// upper envelope R(z) of the convex hull of the (z, r) profile as vertices
+// (vz[i], vR[i]), i = 0..m, z strictly increasing; the outward half-plane of
+// edge e, a_e rho + b_e z <= c_e, as abc[e][3] (a_e > 0); and the n_circle
+// face normals of the polygon revolved at the azimuths 2 pi j / n_circle,
+// divided by cos(pi / n_circle), as g[k][2] (x, y).  A point is inside iff
+// z_min <= z <= z_max and g_k . (x, y) <= R(z) for every k.
+struct JshHull {
+  const double* vz;
+  const double* vR;
+  const double* abc;
+  const double* g;
+  int32_t m, n_circle;
+  double z_min, z_max;
+};
+
 struct JshModel {
   // geometry
   int32_t geo_kind;
@@ -50,6 +66,8 @@ struct JshModel {
   double gdx, gdy, gdz;   // geometry unit direction
   double big_scale, r, r0, z0;
   JshCone cone;           // Cone, or the tangent cone of a ParabaloidCone
+  int32_t hull_id, pad_hull;
+  JshHull hull;           // SimulationGeometry (copy of the context's view)
   // field parameters
   double bp[8], np[8], vp[8];
   // derived field constants

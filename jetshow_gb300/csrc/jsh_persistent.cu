@@ -709,11 +709,15 @@ __global__ void __launch_bounds__(128) transfer_static_mixed_kernel(const JshReq
 }
 
 // Persistent CTAs: each warp keeps 32 lanes busy, refilling idle lanes from
-// the global queue when at least `refill` of them are idle.
-template <bool FULL>
-__global__ void __launch_bounds__(256, 1) transfer_persistent_mixed_kernel(const JshRequest* __restrict__ reqs,
-                                                                         int n_req, unsigned long long* queue,
-                                                                         int refill) {
+// the global queue when at least `refill` of them are idle.  COMPACT builds
+// the kernel for at most 128 threads and 3 resident CTAs per SM, which caps
+// it at 168 registers (154 used, no spills) instead of 198: 12 instead of 10
+// resident warps per SM, more latency hiding for the bulk of short rays at
+// the price of issue slots for the long ones; the autotuner picks.
+template <bool FULL, bool COMPACT>
+__global__ void __launch_bounds__(COMPACT ? 128 : 256, COMPACT ? 3 : 1)
+    transfer_persistent_mixed_kernel(const JshRequest* __restrict__ reqs, int n_req, unsigned long long* queue,
+                                     int refill) {
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
   extern __shared__ float ksh[];
   batch_prefix(reqs, n_req, base);
@@ -777,33 +781,50 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
     rank_scatter_kernel<<<g, 256, 0, stream>>>(d_reqs);
   }
   int bs = shape.block_size;
-  if (bs > 256) bs = 256;
-  int per_sm = shape.ctas_per_sm > 0 ? shape.ctas_per_sm : jsh_persistent_occupancy(JSH_PREC_MIXED, full, bs);
+  if (bs > (shape.compact ? 128 : 256)) bs = shape.compact ? 128 : 256;
+  int per_sm = shape.ctas_per_sm > 0 ? shape.ctas_per_sm
+                                     : jsh_persistent_occupancy(JSH_PREC_MIXED, full, bs, shape.compact);
   if (per_sm < 1) per_sm = 1;
   unsigned blocks = (unsigned)(num_sms * per_sm);
   uint64_t need = (max_items + 31) / 32 * 32;
   if ((uint64_t)blocks * bs > need) blocks = (unsigned)((need + bs - 1) / bs);
   if (blocks == 0) blocks = 1;
   unsigned long long* q = (unsigned long long*)queue;
-  if (full)
-    transfer_persistent_mixed_kernel<true><<<blocks, bs, stage_smem<true>(bs), stream>>>(d_reqs, n_req, q,
-                                                                                       shape.refill_threshold);
-  else
-    transfer_persistent_mixed_kernel<false><<<blocks, bs, stage_smem<false>(bs), stream>>>(d_reqs, n_req, q,
-                                                                                         shape.refill_threshold);
+  const int rf = shape.refill_threshold;
+  if (shape.compact) {
+    if (full)
+      transfer_persistent_mixed_kernel<true, true><<<blocks, bs, stage_smem<true>(bs), stream>>>(d_reqs, n_req, q, rf);
+    else
+      transfer_persistent_mixed_kernel<false, true><<<blocks, bs, stage_smem<false>(bs), stream>>>(d_reqs, n_req, q,
+                                                                                                 rf);
+  } else {
+    if (full)
+      transfer_persistent_mixed_kernel<true, false><<<blocks, bs, stage_smem<true>(bs), stream>>>(d_reqs, n_req, q,
+                                                                                                rf);
+    else
+      transfer_persistent_mixed_kernel<false, false><<<blocks, bs, stage_smem<false>(bs), stream>>>(d_reqs, n_req, q,
+                                                                                                  rf);
+  }
   return cudaGetLastError();
 }
 
 int jsh_queue64_occupancy(int block_size);
 
-int jsh_persistent_occupancy(int precision, bool full, int block_size) {
+int jsh_persistent_occupancy(int precision, bool full, int block_size, bool compact) {
   int n = 0;
   if (precision == JSH_PREC_MIXED) {
-    if (full)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<true>, block_size,
+    if (compact && block_size > 128) return 0;
+    if (compact && full)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<true, true>, block_size,
+                                                    stage_smem<true>(block_size));
+    else if (compact)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<false, true>, block_size,
+                                                    stage_smem<false>(block_size));
+    else if (full)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<true, false>, block_size,
                                                     stage_smem<true>(block_size));
     else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<false>, block_size,
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<false, false>, block_size,
                                                     stage_smem<false>(block_size));
   } else {
     n = jsh_queue64_occupancy(block_size);

@@ -4,7 +4,8 @@ The classes keep the reference constructors (names, argument order and
 meaning) and compile to the C-ABI descriptors of ``include/jetshow_capi.h``:
 
 * geometry: ``Cone`` (include/Cone.h:14-15), ``Cylinder`` (include/Cylinder.h:14-15),
-  ``Parabaloid`` (include/Parabaloid.h:18-19), ``ParabaloidCone`` (include/ParabaloidCone.h:19-20);
+  ``Parabaloid`` (include/Parabaloid.h:18-19), ``ParabaloidCone`` (include/ParabaloidCone.h:19-20),
+  ``SimulationGeometry`` (include/Geometry.h:58-65);
 * fields: include/BField.h:36-208, include/NField.h:10-69, include/VField.h:11-185;
 * ``Jet`` (include/Jet.h:11-61), ``ImagePlane`` (include/ImagePlane.h:22-23),
   ``Observation`` (include/Observation.h:12-24).
@@ -90,6 +91,19 @@ class ParabaloidCone(_Geometry):
     def desc(self):
         return A.GeometryDesc(kind=A.GEO_PARABALOID_CONE, origin=self.origin, direction=self.direction,
                               r0=self.r0, z0=self.z0, big_scale=self.big_scale)
+
+
+class SimulationGeometry(_Geometry):
+    """SimulationGeometry(tree) -- src/Geometry.cpp:92-132: the convex hull of
+    a simulation's (z, r) points revolved about the jet axis (the reference
+    builds ``tree`` from the points at 36 azimuths, src/main.cpp:880-897).
+    ``hull`` is the id returned by ``Context.hull_upload(zr, n_circle)``."""
+
+    def __init__(self, hull):
+        self.hull = int(hull)
+
+    def desc(self):
+        return A.GeometryDesc(kind=A.GEO_SIMULATION, hull_id=self.hull, direction=(0.0, 0.0, 1.0))
 
 
 # --------------------------------------------------------------- fields

@@ -77,7 +77,7 @@ class Context:
         check(self.lib, self.lib.jsh_autotune(self.handle, C.byref(model), C.byref(plane), A.dptr(nu), nu.size,
                                               C.byref(params), C.byref(t)))
         return {"block_size": t.block_size, "ctas_per_sm": t.ctas_per_sm, "refill_threshold": t.refill_threshold,
-                "ms": t.ms}
+                "compact": t.compact, "ms": t.ms}
 
     def last_stats(self):
         st = A.Stats()
@@ -130,6 +130,15 @@ class Context:
                                                  tri.ctypes.data_as(C.POINTER(C.c_int32)), tri.shape[0],
                                                  C.byref(gid)))
         return gid.value
+
+    def hull_upload(self, zr, n_circle: int = 36) -> int:
+        """Build and upload the hull of SimulationGeometry: the (z, r) points
+        [pc] revolved at n_circle azimuths; returns the hull id."""
+        zr = np.ascontiguousarray(zr, dtype=np.float64).reshape(-1, 2)
+        hid = C.c_int32()
+        check(self.lib, self.lib.jsh_hull_upload(self.handle, A.dptr(zr), zr.shape[0], int(n_circle),
+                                                 C.byref(hid)))
+        return hid.value
 
     def grid_interpolate(self, grid_id: int, field: int, zr, nan_value=0.0):
         """Values of field `field` at points (z, r) [pc], interpolated on the device."""

@@ -171,6 +171,7 @@ typedef struct {
   v3 origin, dir;
   double big_scale, r, r0, z0;
   cone_t cone;       /* the cone, or the tangent cone of a ParabaloidCone */
+  int hull;          /* SimulationGeometry: registered hull id */
 } geo_t;
 
 static void cone_init(cone_t* c, v3 origin, v3 dir, double angle, double scale) {
@@ -366,6 +367,194 @@ static void parabaloid_cone_hit(const geo_t* g, v3 ro, v3 rd, hits_t* h) {
   h->s[0].out = pout;
 }
 
+/* --------------------------------------------------------------------
+ * SimulationGeometry (src/Geometry.cpp:92-132; hull built at
+ * src/main.cpp:880-897): the convex hull of the (z, r) points revolved at
+ * n_circle azimuths phi_j = 2 pi j / n_circle, (r sin phi_j, r cos phi_j, z),
+ * intersected with the ray's line in pc.  The hull of such a cloud is
+ * {(x, y, z): max_k g_k . (x, y) <= R(z), z_min <= z <= z_max}, g_k the
+ * face normals of the regular n_circle-gon at (2k + 1) pi / n_circle over
+ * cos(pi / n_circle) and R the upper envelope of the 2-D hull of the (z, r)
+ * points: both support functions are max_i (r_i |u_xy| c(psi) + z_i u_z),
+ * c(psi) = max_j cos(phi_j - psi).  tests/test_hull.py checks the form
+ * against scipy's Qhull hull of the revolved cloud itself.
+ * -------------------------------------------------------------------- */
+#define JO_MAX_HULLS 16
+typedef struct {
+  int used, m, n_circle;
+  double *vz, *vR, *abc, *g;
+  double z_min, z_max;
+} jo_hull;
+static jo_hull g_hulls[JO_MAX_HULLS];
+
+static int cmp_zr(const void* pa, const void* pb) {
+  const double* a = (const double*)pa;
+  const double* b = (const double*)pb;
+  if (a[0] != b[0]) return a[0] < b[0] ? -1 : 1;
+  if (a[1] != b[1]) return a[1] < b[1] ? -1 : 1;
+  return 0;
+}
+
+int jo_hull_register(int32_t hull_id, const double* zr, int64_t n, int32_t n_circle) {
+  if (hull_id < 0 || hull_id >= JO_MAX_HULLS || n < 2 || n_circle < 3 || n_circle > 4096) return JSH_ERR_INVALID;
+  for (int64_t i = 0; i < n; ++i)
+    if (!isfinite(zr[2 * i]) || !isfinite(zr[2 * i + 1]) || zr[2 * i + 1] < 0) return JSH_ERR_INVALID;
+  double* p = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+  memcpy(p, zr, sizeof(double) * 2 * (size_t)n);
+  qsort(p, (size_t)n, 2 * sizeof(double), cmp_zr);
+  /* per z only its largest r can lie on the upper envelope */
+  int64_t nq = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (i + 1 < n && p[2 * (i + 1)] == p[2 * i]) continue;
+    p[2 * nq] = p[2 * i];
+    p[2 * nq + 1] = p[2 * i + 1];
+    nq++;
+  }
+  if (nq < 2) { free(p); return JSH_ERR_INVALID; }
+  /* Andrew's monotone chain, upper hull of (z, r); collinear points dropped */
+  double* h = (double*)malloc(sizeof(double) * 2 * (size_t)nq);
+  int64_t nh = 0;
+  for (int64_t i = 0; i < nq; ++i) {
+    double cz = p[2 * i], cr = p[2 * i + 1];
+    while (nh >= 2) {
+      double oz = h[2 * (nh - 2)], orr = h[2 * (nh - 2) + 1], az = h[2 * (nh - 1)], ar = h[2 * (nh - 1) + 1];
+      double cross = (az - oz) * (cr - orr) - (ar - orr) * (cz - oz);
+      if (cross >= 0) nh--;
+      else break;
+    }
+    h[2 * nh] = cz;
+    h[2 * nh + 1] = cr;
+    nh++;
+  }
+  free(p);
+  jo_hull* H = &g_hulls[hull_id];
+  if (H->used) { free(H->vz); free(H->vR); free(H->abc); free(H->g); }
+  int m = (int)(nh - 1);
+  H->m = m;
+  H->n_circle = n_circle;
+  H->vz = (double*)malloc(sizeof(double) * (size_t)(m + 1));
+  H->vR = (double*)malloc(sizeof(double) * (size_t)(m + 1));
+  H->abc = (double*)malloc(sizeof(double) * 3 * (size_t)m);
+  H->g = (double*)malloc(sizeof(double) * 2 * (size_t)n_circle);
+  for (int i = 0; i <= m; ++i) { H->vz[i] = h[2 * i]; H->vR[i] = h[2 * i + 1]; }
+  free(h);
+  for (int e = 0; e < m; ++e) {
+    double a = H->vz[e + 1] - H->vz[e];
+    double b = -(H->vR[e + 1] - H->vR[e]);
+    H->abc[3 * e] = a;
+    H->abc[3 * e + 1] = b;
+    H->abc[3 * e + 2] = a * H->vR[e] + b * H->vz[e];
+  }
+  double inv_cos = 1.0 / cos(JO_PI / (double)n_circle);
+  for (int k = 0; k < n_circle; ++k) {
+    double ang = ((2.0 * k + 1.0) * JO_PI) / (double)n_circle;
+    H->g[2 * k] = sin(ang) * inv_cos;
+    H->g[2 * k + 1] = cos(ang) * inv_cos;
+  }
+  H->z_min = H->vz[0];
+  H->z_max = H->vz[m];
+  H->used = 1;
+  return JSH_OK;
+}
+
+int jo_hull_profile(int32_t hull_id, double* vz, double* vR, int32_t* m) {
+  if (hull_id < 0 || hull_id >= JO_MAX_HULLS || !g_hulls[hull_id].used) return JSH_ERR_NOT_FOUND;
+  const jo_hull* H = &g_hulls[hull_id];
+  if (m) *m = H->m;
+  for (int i = 0; i <= H->m; ++i) {
+    if (vz) vz[i] = H->vz[i];
+    if (vR) vR[i] = H->vR[i];
+  }
+  return JSH_OK;
+}
+
+/* D(z_i) = R_i - (A + B z_i): R minus the line's sector coordinate */
+static double hull_D(const jo_hull* H, int i, double A, double B) { return H->vR[i] - (A + B * H->vz[i]); }
+
+static double hull_edge_t(const jo_hull* H, int e, double u0, double u1, double oz, double dz) {
+  double a = H->abc[3 * e], b = H->abc[3 * e + 1], c = H->abc[3 * e + 2];
+  double alpha = (a * u0 + b * oz) - c;
+  double beta = a * u1 + b * dz;
+  if (beta == 0.0) return (H->vz[e] - oz) / dz;
+  return -alpha / beta;
+}
+
+/* Per sector k the line's slab interval: along z (d_z != 0) D is concave
+ * and piecewise linear with breaks at the profile vertices; its maximum
+ * vertex and the sign changes on both sides (binary searches) give the
+ * crossed edges (or the caps z_min, z_max).  The segment is
+ * [max_k t_in, min_k t_out]; point_in is the point of smaller t. */
+static void simulation_hit(const jo_hull* H, v3 ro_cm, v3 rd, hits_t* h) {
+  v3 o = vdiv(ro_cm, JO_PC);
+  int m = H->m;
+  double tlo = -INFINITY, thi = INFINITY;
+  if (rd.z == 0.0) {
+    if (!(o.z >= H->z_min && o.z <= H->z_max)) return;
+    int lo = 0, hi = m;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (H->vz[mid] <= o.z) lo = mid;
+      else hi = mid;
+    }
+    double a = H->abc[3 * lo], b = H->abc[3 * lo + 1], c = H->abc[3 * lo + 2];
+    double R0 = (c - b * o.z) / a;
+    for (int k = 0; k < H->n_circle; ++k) {
+      double gx = H->g[2 * k], gy = H->g[2 * k + 1];
+      double u0 = gx * o.x + gy * o.y, u1 = gx * rd.x + gy * rd.y;
+      if (u1 > 0.0) thi = fmin(thi, (R0 - u0) / u1);
+      else if (u1 < 0.0) tlo = fmax(tlo, (R0 - u0) / u1);
+      else if (u0 > R0) return;
+    }
+  } else {
+    double t_zmin = (H->z_min - o.z) / rd.z, t_zmax = (H->z_max - o.z) / rd.z;
+    for (int k = 0; k < H->n_circle; ++k) {
+      double gx = H->g[2 * k], gy = H->g[2 * k + 1];
+      double u0 = gx * o.x + gy * o.y, u1 = gx * rd.x + gy * rd.y;
+      double B = u1 / rd.z, A = u0 - B * o.z;
+      int lo = 0, hi = m;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if ((H->vR[mid + 1] - H->vR[mid]) - B * (H->vz[mid + 1] - H->vz[mid]) < 0.0) hi = mid;
+        else lo = mid + 1;
+      }
+      int top = lo;
+      if (!(hull_D(H, top, A, B) >= 0.0)) return;
+      double ta, tb;
+      if (hull_D(H, 0, A, B) >= 0.0) {
+        ta = t_zmin;
+      } else {
+        int l = 0, r = top;
+        while (r - l > 1) {
+          int mid = (l + r) >> 1;
+          if (hull_D(H, mid, A, B) >= 0.0) r = mid;
+          else l = mid;
+        }
+        ta = hull_edge_t(H, l, u0, u1, o.z, rd.z);
+      }
+      if (hull_D(H, m, A, B) >= 0.0) {
+        tb = t_zmax;
+      } else {
+        int l = top, r = m;
+        while (r - l > 1) {
+          int mid = (l + r) >> 1;
+          if (hull_D(H, mid, A, B) >= 0.0) l = mid;
+          else r = mid;
+        }
+        tb = hull_edge_t(H, l, u0, u1, o.z, rd.z);
+      }
+      tlo = fmax(tlo, fmin(ta, tb));
+      thi = fmin(thi, fmax(ta, tb));
+    }
+  }
+  if (!(tlo < thi)) {
+    if (tlo == thi) h->status |= JSH_ST_UB_GEOMETRY;
+    return;
+  }
+  h->n = 1;
+  h->s[0].in = vmul(ray_point(o, rd, tlo), JO_PC);
+  h->s[0].out = vmul(ray_point(o, rd, thi), JO_PC);
+}
+
 static int geo_init(const jsh_geometry_desc* d, geo_t* g) {
   memset(g, 0, sizeof(*g));
   g->kind = d->kind;
@@ -382,6 +571,10 @@ static int geo_init(const jsh_geometry_desc* d, geo_t* g) {
       return JSH_OK;
     case JSH_GEO_CYLINDER:
     case JSH_GEO_PARABALOID:
+      return JSH_OK;
+    case JSH_GEO_SIMULATION:
+      if (d->hull_id < 0 || d->hull_id >= JO_MAX_HULLS || !g_hulls[d->hull_id].used) return JSH_ERR_NOT_FOUND;
+      g->hull = d->hull_id;
       return JSH_OK;
     case JSH_GEO_PARABALOID_CONE: {
       /* tangent cone at z0 (src/ParabaloidCone.cpp:12-18) */
@@ -405,6 +598,7 @@ static void geo_hit(const geo_t* g, v3 ro, v3 rd, hits_t* h) {
     case JSH_GEO_CYLINDER: cylinder_hit(g, ro, rd, h); break;
     case JSH_GEO_PARABALOID: parabaloid_hit(g->r0, ro, rd, h); break;
     case JSH_GEO_PARABALOID_CONE: parabaloid_cone_hit(g, ro, rd, h); break;
+    case JSH_GEO_SIMULATION: simulation_hit(&g_hulls[g->hull], ro, rd, h); break;
     default: break;
   }
 }

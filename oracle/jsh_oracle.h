@@ -80,6 +80,12 @@ int jo_grid_register(int32_t grid_id, const double* xy, int64_t n,
 double jo_grid_value(int32_t grid_id, int32_t field, double z_pc, double r_pc,
                      double nan_value);
 
+/* Register the hull of SimulationGeometry under hull_id (0..15): the (z, r)
+ * points zr[n][2] in pc revolved at n_circle azimuths. */
+int jo_hull_register(int32_t hull_id, const double* zr, int64_t n, int32_t n_circle);
+/* Vertices of a registered hull's profile R(z): vz, vR [m+1] (may be NULL). */
+int jo_hull_profile(int32_t hull_id, double* vz, double* vR, int32_t* m);
+
 int jo_openmp_threads(void);
 
 #ifdef __cplusplus

@@ -64,6 +64,8 @@ def lib():
                                        P(C.c_int32), C.c_int64]
         L.jo_grid_value.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double]
         L.jo_grid_value.restype = C.c_double
+        L.jo_hull_register.argtypes = [C.c_int32, D, C.c_int64, C.c_int32]
+        L.jo_hull_profile.argtypes = [C.c_int32, D, D, P(C.c_int32)]
         L.jo_openmp_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -150,6 +152,20 @@ def grid_register(grid_id, xy, values, tri):
 
 def grid_value(grid_id, field, z_pc, r_pc, nan_value=0.0):
     return lib().jo_grid_value(grid_id, field, z_pc, r_pc, nan_value)
+
+
+def hull_register(hull_id, zr, n_circle=36):
+    zr = np.ascontiguousarray(zr, dtype=np.float64).reshape(-1, 2)
+    _chk(lib().jo_hull_register(hull_id, A.dptr(zr), zr.shape[0], int(n_circle)))
+
+
+def hull_profile(hull_id):
+    """(z, R) vertices of a registered hull's profile."""
+    m = C.c_int32()
+    _chk(lib().jo_hull_profile(hull_id, None, None, C.byref(m)))
+    vz = np.zeros(m.value + 1); vr = np.zeros(m.value + 1)
+    _chk(lib().jo_hull_profile(hull_id, A.dptr(vz), A.dptr(vr), C.byref(m)))
+    return vz, vr
 
 
 def threads():

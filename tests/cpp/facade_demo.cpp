@@ -1,7 +1,8 @@
 // A reference-style caller of the C++ facade: builds the conical jet of the
 // parity tests with the reference's class names, renders "I" and "full" on
 // the GPU, writes the planes to a binary file (argv[1]) for comparison with
-// the Python binding, and checks the error paths throw.
+// the Python binding, renders the jet inside a SimulationGeometry hull, and
+// checks the error paths throw.
 #include <cmath>
 #include <cstdio>
 #include <stdexcept>
@@ -60,6 +61,17 @@ int main(int argc, char** argv) {
   } catch (const std::runtime_error&) {
     ++thrown;
   }
+  try {
+    SimulationGeometry flat({1.0, 0.1, 1.0, 0.2});  // one z: a flat hull
+  } catch (const std::runtime_error&) {
+    ++thrown;
+  }
+  // the conical jet bounded by the revolved hull of a (z, r) rectangle
+  SimulationGeometry hull({0.0, 0.0, 0.0, 2.0, 40.0, 0.0, 40.0, 2.0});
+  Jet hulljet(&hull, &vfield, &bfield, &nfield, 2.5, 10.0);
+  Observation in_hull(&hulljet, &imagePlane, 15.4e9 * 1.1);
+  in_hull.run(100, 1e4, 0.0, 1e-10, "adaptive", "I");
+  std::printf("hull: hit pixels %llu\n", (unsigned long long)in_hull.stats().n_hit_pixels);
   std::printf("thrown %d\n", thrown);
-  return thrown == 3 ? 0 : 1;
+  return thrown == 4 ? 0 : 1;
 }

@@ -35,7 +35,8 @@ def test_facade_matches_python_binding(lib, ctx, tmp_path):
     out = tmp_path / "planes.bin"
     r = subprocess.run([exe, str(out)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "thrown 3" in r.stdout
+    assert "thrown 4" in r.stdout
+    assert "hull: hit pixels 0" not in r.stdout
     got = np.fromfile(out, dtype=np.float64).reshape(2, 5, 32, 32)
     jet = J.Jet(J.Cone((0., 0., 0.), (0., 0., 1.), 0.05, 100. * J.pc), J.ConstFlatVField(10.),
                 J.HelicalConicalBField(0.1, 1.0, math.pi / 4, True), J.BKNField(500., 2., True), s=2.5,

@@ -19,7 +19,13 @@ def test_autotune_shape_and_invariance(ctx):
     t = ctx.autotune(jet.desc(), plane.desc(), nu, p)
     assert t["block_size"] in (64, 96, 128, 192, 256)
     assert t["ctas_per_sm"] >= 1 and 1 <= t["refill_threshold"] <= 32 and t["ms"] > 0
+    assert t["compact"] in (0, 1)
     after, st = ctx.render(jet.desc(), plane.desc(), nu, p)
     assert st["n_work_items"] > 0
+    # the register-capped build of the kernel, explicitly
+    compact = J.make_params(precision="mixed", schedule="persistent", block_size=96, ctas_per_sm=3,
+                            refill_threshold=8, flags=J.A.FLAG_COMPACT_REGS, **W.ACCURATE_KW)
+    capped, _ = ctx.render(jet.desc(), plane.desc(), nu, compact)
     for k in ("tau", "I", "Q", "U", "V", "status"):
         assert np.array_equal(before[k], after[k]), k
+        assert np.array_equal(before[k], capped[k]), k
