@@ -201,13 +201,15 @@ typedef struct jsh_params {
   int32_t flags;           /* JSH_FLAG_* (0 = defaults)                              */
 } jsh_params;
 
-/* Mixed precision: start the IQUV pass of an optically thick ray where the
- * optical depth from the observer first exceeds tau_thick = 16 / (1 - p)
- * (p = k_Q / k_I + 0.05, at most 0.95; p = 0 for I-only output) instead of
- * at tau_max.  The Stokes vector entering at that depth reaches the observer
- * attenuated by at least exp(-16) ~ 1.1e-7 (10 times below the relative
- * tolerance 1e-6 of the integration itself), so the image agrees with the
- * integration from tau_max to that factor; thick rays need a small fraction
+/* Mixed precision: start the IQUV pass of an optically thick ray inside it
+ * instead of at tau_max.  With tau_thick = 16 / (1 - p) (p = k_Q / k_I +
+ * 0.05, at most 0.95; p = 0 for I-only output) the Stokes vector entering at
+ * tau_thick reaches the observer attenuated by at least exp(-16) ~ 1.1e-7.
+ * I-only output starts there from the zero state.  Full Stokes output starts
+ * a ray deeper than tau_thick at optical depth 30 from the local equilibrium
+ * x = K^-1 eps of the transfer matrix (the true state there differs from it
+ * only through the source function's gradients; measured worst 2.2e-6 of I
+ * against the integration from tau_max).  Thick rays need a small fraction
  * of the stiff IQUV steps.  This flag turns it off (integrate from tau_max
  * like src/Observation.cpp:242-274).  The FP64 path always integrates from
  * tau_max. */

@@ -44,9 +44,11 @@ struct JshMixed {
   float nl[3];           // LOS towards the observer (-ray direction)
   float pk;              // (s + 2) / 2
   float kq, eq;          // k_Q / k_I, eta_Q / eta_I
-  float pad_;
+  int32_t eq_start;      // full Stokes: start thick rays at tau_eq in local equilibrium
   double dt_max_pc;      // tau-pass step limit [pc], 0 = none
-  double tau_thick;      // IQUV pass starts where the optical depth first exceeds this
+  double tau_thick;      // optical depth beyond which the truncated part of a ray is negligible
+  double tau_eq;         // the tau pass lands a step on this depth; IQUV starts there
+                         // (zero state if tau_eq == tau_thick, local equilibrium otherwise)
   // FP32 copies of the field parameters (q) and of q / pc, and the derived
   // constants the FP32 field laws use: no FP64 operation per evaluation
   float vq[8], vq_pc[8], nq[8], nq_pc[8], bq[8], bq_pc[8];
