@@ -313,9 +313,68 @@ __device__ __forceinline__ void coef32_tail(const JshFreqConst& F, const JshMixe
   c.kC = -F.ac * np_ * (F.c1 * w * w - F.c2 * P);
 }
 
-__device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqConst& F, F3 p, bool full, Coef32& c) {
+// Which coefficients coef32_rt computes: k_I only (the tau pass), k_I and
+// eta_I (I-only output), all of them.  k_I comes out bitwise the same in
+// every mode, so an item's tau does not depend on the modes its warp-mates
+// force on it.
+enum CoefMode { COEF_KI = 0, COEF_I = 1, COEF_FULL = 2 };
+
+// The benchmark family in the plasma frame (ConstFlat V, helical conical B,
+// BK n) in the log domain: with l = log2|p|, u the helical unit direction
+// and w = |n' x B| D = b |n' x u| D,
+//   log2 n' = log2 n0' - m_n l,   log2 w = log2(b0 D) - m_b l + log2 |n' x u|,
+//   k_I = a_k n' 2^(pk log2 w),  eta_I = a_e D n' 2^((pk - 1/2) log2 w)
+// (pk = (s + 2) / 2): the tau pass's k_I costs two log2, one rsqrt and two
+// exp2 instead of eight MUFU operations.  The other coefficients follow
+// from k_I, eta_I, n', b and w: k_V = -(a_V / a_e) B_par eta_I, eta_V =
+// -(a_eV / a_k) B_par D^2 k_I / w, k_F = a_F n' B_par D, k_C = -a_C c1 n' w^2
+// + (a_C c2 / a_k) k_I, B_par = b (u . n').
+__device__ __forceinline__ void coef32_helical_log(const JshMixed& X, const JshFreqConst& F, F3 p, int mode,
+                                                   Coef32& c) {
+  const float l = 0.5f * __log2f(fdot(p, p));
+  const float rc2 = p.x * p.x + p.y * p.y;
+  float px = 0.f, py = 0.f;
+  if (rc2 > 0.f) {
+    const float irc = rsqrtf(rc2);
+    px = -p.y * irc;
+    py = p.x * irc;
+    if (X.bq[3] != 0.f && p.x < 0.f) {
+      px = -px;
+      py = -py;
+    }
+  }
+  const float st = X.b_sign * X.sin_pitch;
+  const F3 u = f3(st * px, st * py, X.b_sign * X.cos_pitch);
+  const F3 nlp = f3(X.nlp[0], X.nlp[1], X.nlp[2]);
+  const F3 cr = fcross(nlp, u);
+  const float lw = fmaf(-X.bq[1], l, X.l2_b0D) + 0.5f * __log2f(fdot(cr, cr));
+  // n' and w^pk as two exp2 of arguments of ~20 each rather than one of ~50:
+  // exp2f's relative error is ~ulp(argument), so the split keeps k_I's
+  // rounding at the level of the product form
+  const float n_ = exp2f(fmaf(-X.nq[1], l, X.l2_n0));
+  c.kI = (F.ak * n_) * exp2f(X.pk * lw);
+  if (mode == COEF_KI) return;
+  c.eI = (F.ae * X.D * n_) * exp2f(X.pk_h * lw);
+  if (mode == COEF_I) return;
+  const float bpar = exp2f(fmaf(-X.bq[1], l, X.l2_b0)) * fdot(u, nlp);
+  const float w = exp2f(lw);
+  const float D = X.D;
+  c.kQ = X.kq * c.kI;
+  c.eQ = X.eq * c.eI;
+  c.kV = -F.r_kv * bpar * c.eI;
+  c.eV = (w > 0.f) ? -F.r_ev * bpar * (D * D) * (c.kI / w) : 0.f;
+  c.kF = F.af * n_ * bpar * D;
+  c.kC = fmaf(F.r_kc, c.kI, -F.ac * F.c1 * n_ * (w * w));
+}
+
+__device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqConst& F, F3 p, int mode, Coef32& c) {
   const JshModel& m = R.model;
   const JshMixed& X = R.mix;
+  if (X.helical_log) {
+    coef32_helical_log(X, F, p, mode, c);
+    return;
+  }
+  const bool full = mode == COEF_FULL;
   float D, gamma, beta, np_;
   F3 nlp, vdir, B;
   if (X.helical_bk) {

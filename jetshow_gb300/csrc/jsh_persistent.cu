@@ -50,6 +50,11 @@ constexpr uint8_t PH_IDLE = 0, PH_TAU = 1, PH_IQUV = 2;
 // worst 2.2e-6 of I in I, Q, U, V at tau_eq = 30 (2.6e-5 at 20), against
 // 3e-10 for the zero state at tau_thick = 89.
 constexpr double kTauEq = 30.0;
+// Smallest total depth of a ray started in equilibrium at kTauEq: behind the
+// start lie at least 20 optical depths, so the state there is within
+// exp(-(1 - p) 20) of equilibrium before the 30 depths in front attenuate it
+// (in a uniform medium the error is exp(-(1 - p) 50) ~ 1e-6 of I).
+constexpr double kTauEqMin = 50.0;
 constexpr double INV_PC = 1.0 / JSH_PC;
 
 // Tableau entry a_sj in FP32 (row 6 = the 5th-order weights b), folded to an
@@ -183,11 +188,18 @@ __device__ __forceinline__ double seg_len_cm(const JshHit& H, int s, double ox, 
   return sqrt((dx * dx + dy * dy) + dz * dz);
 }
 
-__device__ __noinline__ double first_step_divisor(double tau_bg, int n) {
-  // auto_n of src/Observation.cpp:254-258
-  double auto_n = n;
-  if (tau_bg > 0.1) auto_n = steps_schedule(tau_bg, n, 10 * n);
-  return auto_n;
+// auto_n of src/Observation.cpp:254-258: steps_schedule (src/utils.cpp:354-366,
+// default limits 0.1 and 100) in FP32.  It only sets the first step guess of
+// a segment, so FP32 rounding near an integer boundary changes no accuracy;
+// in FP64 its log and pow were a large share of the per-item FP64 work
+// (GB300 runs FP64 at 1/64 of the FP32 rate).
+__device__ __forceinline__ float first_step_divisor(double tau_bg, int n) {
+  if (!(tau_bg > 0.1)) return (float)n;
+  if (tau_bg >= 100.0) return (float)(10 * n);
+  const float b = 2.30258509f;                              // -log(0.1)
+  const float k = (float)(10 * n) / ((4.60517019f + b) * (4.60517019f + b));  // log(100) + b
+  const float l = logf((float)tau_bg) + b;
+  return ceilf(fmaf(k * l, l, (float)n));
 }
 
 __device__ __forceinline__ void set_segment(Lane& L, double ox, double oy, double oz, double length_cm) {
@@ -210,7 +222,7 @@ __device__ __forceinline__ void set_segment(Lane& L, double ox, double oy, doubl
 __device__ __forceinline__ void begin_tau_segment(Lane& L, const JshRequest& R, const JshHit& H) {
   int s = L.seg;
   set_segment(L, H.seg[s][0], H.seg[s][1], H.seg[s][2], seg_len_cm(H, s, H.seg[s][3], H.seg[s][4], H.seg[s][5]));
-  L.dt = (float)(df_val(L.length) / R.P.n);
+  L.dt = (L.length.hi + L.length.lo) / (float)R.P.n;
   L.tau_seg = DF{0.f, 0.f};
   L.thick_left = (float)(R.mix.tau_eq - L.tau_bg);
 }
@@ -226,7 +238,7 @@ __device__ __forceinline__ void begin_iquv_segment(Lane& L, const JshRequest& R,
     oz = H.seg[s][2] + R.plane.rz * tc;
   }
   set_segment(L, ox, oy, oz, seg_len_cm(H, s, ox, oy, oz));
-  L.dt = (float)(df_val(L.length) / first_step_divisor(L.tau_bg, R.P.n));
+  L.dt = (L.length.hi + L.length.lo) / first_step_divisor(L.tau_bg, R.P.n);
 }
 
 // Work item w of the batch.  Unranked: frequency-major over the hit list.
@@ -266,21 +278,23 @@ __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict
 // Writes one finished item (the Stokes vector rotated back to the lab frame
 // in FP64) and its counters.
 __device__ __noinline__ void write_finished(const JshRequest* __restrict__ reqs, int r, int f, uint32_t h,
-                                            double tau_bg, double thick, double chi, float x0, float x1, float x2,
-                                            float x3, uint32_t status, uint32_t evals, uint32_t acc,
-                                            uint32_t rej) {
+                                            double tau_bg, double thick, float chi_hi, float chi_lo, float x0,
+                                            float x1, float x2, float x3, uint32_t status, uint32_t evals,
+                                            uint32_t acc, uint32_t rej) {
   const JshRequest& R = reqs[r];
   const JshHit& H = R.hits[h];
   uint64_t q = (uint64_t)f * R.npix + (uint64_t)H.pix;
   double S = R.mix.fc[f].scale;
-  double sc, ss;
-  sincos(chi, &ss, &sc);
-  double qq = x1, uu = x2;
+  // rotation by chi = hi + lo (|hi| <= pi): sin, cos of hi in FP32 and the
+  // first-order correction for lo; (Q, U) need ~1e-7 of P, far above this
+  float sh, ch;
+  sincosf(chi_hi, &sh, &ch);
+  const float ss = fmaf(chi_lo, ch, sh), sc = fmaf(-chi_lo, sh, ch);
   if (R.tau) R.tau[q] = tau_bg;
   if (R.l) R.l[q] = (R.P.flags & JSH_FLAG_COST_MAP) ? (double)evals : thick;
   if (R.I) R.I[q] = S * (double)x0;
-  if (R.Q) R.Q[q] = S * (sc * qq - ss * uu);
-  if (R.U) R.U[q] = S * (ss * qq + sc * uu);
+  if (R.Q) R.Q[q] = S * (double)fmaf(sc, x1, -ss * x2);
+  if (R.U) R.U[q] = S * (double)fmaf(ss, x1, sc * x2);
   if (R.V) R.V[q] = S * (double)x3;
   if (R.status) R.status[q] = status;
   unsigned long long* c = R.counters;
@@ -291,8 +305,8 @@ __device__ __noinline__ void write_finished(const JshRequest* __restrict__ reqs,
 }
 
 __device__ __forceinline__ void lane_finish(Lane& L, const JshRequest* __restrict__ reqs) {
-  write_finished(reqs, L.r, L.f, L.h, L.tau_bg, L.thick, df_val(L.chi), L.x[0], L.x[1], L.x[2], L.x[3], L.status,
-                 L.evals, L.acc, L.rej);
+  write_finished(reqs, L.r, L.f, L.h, L.tau_bg, L.thick, L.chi.hi, L.chi.lo, L.x[0], L.x[1], L.x[2], L.x[3],
+                 L.status, L.evals, L.acc, L.rej);
   L.phase = PH_IDLE;
 }
 
@@ -319,13 +333,14 @@ __device__ __noinline__ double crossing_time(double tau_old, double t_old, doubl
 }
 
 // Coefficients (one call site per kernel); `full` = false stops after
-// k_I, eta_I (the tau pass, or I-only output).  Returns the magnitude of
-// the terms summed into the derivatives (eta_I + k_I |I| for the Stokes
-// vector, k_I for tau): the scale of their FP32 rounding noise.
-__device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& F, bool tau, bool full, F3 p,
-                                       const float* y, float cs, float sn, float* dk, float& kI) {
+// k_I, eta_I (I-only output, or a tau lane among IQUV lanes), `kionly`
+// (every active lane of the warp in its tau pass) after k_I.  Returns the
+// magnitude of the terms summed into the derivatives (eta_I + k_I |I| for
+// the Stokes vector, k_I for tau): the scale of their FP32 rounding noise.
+__device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& F, bool tau, bool full, bool kionly,
+                                       F3 p, const float* y, float cs, float sn, float* dk, float& kI) {
   Coef32 c;
-  coef32_rt(R, F, p, full, c);
+  coef32_rt(R, F, p, kionly ? COEF_KI : (full ? COEF_FULL : COEF_I), c);
   kI = c.kI;
   if (tau) {
     dk[0] = c.kI;
@@ -365,7 +380,7 @@ __device__ __noinline__ float4 equilibrium_state(const JshRequest* __restrict__ 
                                                 double oy, double oz) {
   const JshRequest& R = reqs[r];
   Coef32 c;
-  coef32_rt(R, R.mix.fc[f], f3((float)(ox * INV_PC), (float)(oy * INV_PC), (float)(oz * INV_PC)), true, c);
+  coef32_rt(R, R.mix.fc[f], f3((float)(ox * INV_PC), (float)(oy * INV_PC), (float)(oz * INV_PC)), COEF_FULL, c);
   double A[4][5] = {{c.kI, c.kQ, 0.0, c.kV, c.eI},
                     {c.kQ, c.kI, c.kF, 0.0, c.eQ},
                     {0.0, -c.kF, c.kI, c.kC, 0.0},
@@ -449,7 +464,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     const float h = L.dt;
     float dk[5];
     if (!L.init) {
-      L.s1 = rhs32(R, F, tau, coef_full, pn, L.x, c0, s0, dk, L.kI1);
+      L.s1 = rhs32(R, F, tau, coef_full, tau && warp_tau, pn, L.x, c0, s0, dk, L.kI1);
 #pragma unroll
       for (int c = 0; c < NK; ++c) L.k1[c] = dk[c];
       L.evals++;
@@ -473,7 +488,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
         cs = c0 * cd - s0 * sd;
         sn = s0 * cd + c0 * sd;
       }
-      const float sc = rhs32(R, F, tau, coef_full, pn + dirf * (c_C[s] * h), y, cs, sn, dk, kI7);
+      const float sc = rhs32(R, F, tau, coef_full, tau && warp_tau, pn + dirf * (c_C[s] * h), y, cs, sn, dk, kI7);
       smax = fmaxf(smax, sc);
       s7 = sc;
 #pragma unroll
@@ -661,8 +676,8 @@ start_iquv : {
   bool eq = false;
   if (L.first_seg >= 0 && R.mix.eq_start) {
     // the equilibrium start needs depth behind tau_eq: rays shallower than
-    // tau_thick are integrated whole from their far end
-    if (L.tau_bg >= R.mix.tau_thick || (L.status & JSH_ST_TAU_CROSSED)) eq = true;
+    // eq_min are integrated whole from their far end
+    if (L.tau_bg >= R.mix.eq_min || (L.status & JSH_ST_TAU_CROSSED)) eq = true;
     else L.first_seg = -1;
   }
   L.seg = L.first_seg >= 0 ? L.first_seg : L.nseg - 1;
@@ -719,7 +734,7 @@ __global__ void __launch_bounds__(256) rank_cost_kernel(const JshRequest* __rest
 #pragma unroll 1
       for (int k = 0; k < 4; ++k) {
         Coef32 c;
-        coef32_rt(R, F, a + d * xk[k], false, c);
+        coef32_rt(R, F, a + d * xk[k], COEF_KI, c);
         acc = fmaf(wk[k], c.kI, acc);
       }
       tau = fmaf(acc, sqrtf(fdot(d, d)), tau);
@@ -968,6 +983,7 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
     // the gradients of the source function, attenuated by exp(-(1 - p) 30)
     X.eq_start = (req->P.full && X.tau_thick < INFINITY && kTauEq < X.tau_thick) ? 1 : 0;
     X.tau_eq = X.eq_start ? kTauEq : X.tau_thick;
+    X.eq_min = X.eq_start ? std::min(kTauEqMin, X.tau_thick) : X.tau_thick;
   }
   if (m.v_kind == JSH_V_CONST_FLAT) {
     // getG, getD, get_n_los_prime (src/utils.cpp:147-162) in FP64
@@ -979,6 +995,15 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
     double f = (D + 1.) * (gamma / (gamma + 1.));
     X.v_const = 1;
     X.helical_bk = (m.b_kind == JSH_B_HELICAL_CONICAL && m.n_kind == JSH_N_BK) ? 1 : 0;
+    const double n0p = m.n_plasma ? m.np[0] : m.np[0] / gamma;
+    X.helical_log = (X.helical_bk && m.b_plasma && m.bp[0] != 0.0 && n0p > 0.0) ? 1 : 0;
+    if (X.helical_log) {
+      X.l2_b0 = (float)log2(fabs(m.bp[0]));
+      X.l2_b0D = (float)log2(fabs(m.bp[0]) * D);
+      X.l2_n0 = (float)log2(n0p);
+      X.pk_h = (float)((s + 1.) / 2.);
+      X.b_sign = m.bp[0] > 0.0 ? 1.f : -1.f;
+    }
     X.D = (float)D;
     X.gamma = (float)gamma;
     X.beta = (float)beta;
@@ -1012,8 +1037,11 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
     F.c2 = (float)(m.kcr_a * Gnu);
     F.scale = S;
     F.atol = (float)(req->P.atol / S);
+    F.r_kv = (float)((Av * JSH_PC) / (Ae * JSH_PC / S));
+    F.r_ev = (float)((Aev * JSH_PC / S) / (Ak * JSH_PC));
+    F.r_kc = (float)((Ac * JSH_PC) * (m.kcr_a * Gnu) / (Ak * JSH_PC));
     if (F.atol == 0.f && req->P.atol > 0.0) F.atol = FLT_MIN;  // below FP32 range: the smallest normal
-    const float vals[6] = {F.ak, F.ae, F.av, F.aev, F.af, F.ac};
+    const float vals[9] = {F.ak, F.ae, F.av, F.aev, F.af, F.ac, F.r_kv, F.r_ev, F.r_kc};
     for (float x : vals) {
       if (!isfinite(x) || (x != 0.f && fabsf(x) < 1e-30f)) {
         jsh_set_error("frequency %g Hz puts the mixed-precision coefficients outside FP32 range; use FP64", nu);

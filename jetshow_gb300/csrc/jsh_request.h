@@ -31,13 +31,20 @@ struct JshFreqConst {
   float ak, ae, av, aev, af, ac, c1, c2;
   double scale;  // S: cgs intensity of one unit of the scaled state
   float atol;    // I/IQUV-pass atol / S
-  float pad_;
+  float r_kv;    // a_V / a_e      (log-domain helical path)
+  float r_ev;    // a_eV / a_k
+  float r_kc;    // a_C c2 / a_k
 };
 
 // Mixed precision, per request.
 struct JshMixed {
   int32_t v_const;       // ConstFlat velocity: Doppler factor and aberrated LOS are constants
   int32_t helical_bk;    // ConstFlat V, helical conical B, BK n: the fused field path
+  int32_t helical_log;   // ... with B in the plasma frame: the log-domain coefficients
+  float l2_b0, l2_b0D;   // log2 |b0|, log2(|b0| D)
+  float l2_n0;           // log2 of n0 in the plasma frame (n0 / Gamma if given in the lab)
+  float pk_h;            // (s + 1) / 2
+  float b_sign;          // sign of b0
   int32_t sim_shared;    // V, N and B all from one grid: one point location per evaluation
   float D, gamma, beta;  // of the constant velocity
   float nlp[3];          // aberrated LOS of the constant velocity
@@ -49,6 +56,7 @@ struct JshMixed {
   double tau_thick;      // optical depth beyond which the truncated part of a ray is negligible
   double tau_eq;         // the tau pass lands a step on this depth; IQUV starts there
                          // (zero state if tau_eq == tau_thick, local equilibrium otherwise)
+  double eq_min;         // equilibrium start only for rays at least this deep
   // FP32 copies of the field parameters (q) and of q / pc, and the derived
   // constants the FP32 field laws use: no FP64 operation per evaluation
   float vq[8], vq_pc[8], nq[8], nq_pc[8], bq[8], bq_pc[8];
