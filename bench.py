@@ -37,12 +37,24 @@ METRIC = "full_stokes_rays_per_s"
 UNIT = "rays/s"
 WORKLOAD = ("conical jet 512x1024 log-spaced (lg mas -3..-1), 4 freq (8.1/8.4/12.1/15.4 GHz), full Stokes, "
             "rtol 1e-6 with atol tightened to the 1e-4-qualified tolerances")
-# source-level op census of one mixed-precision full-Stokes right-hand-side
-# evaluation of this workload's model (ConstFlat V, helical conical B, BK n),
-# stage combination and error estimate amortised over the 6 evaluations of a
-# step: FP32 arithmetic instructions (an FMA counts once) and MUFU ops
+# source-level op census of one mixed-precision right-hand-side evaluation
+# of this workload's model (ConstFlat V, helical conical B, BK n), stage
+# combination and error estimate amortised over the 6 evaluations of a step:
+# FP32 arithmetic instructions (an FMA counts once) and MUFU ops.  A
+# full-Stokes evaluation (IQUV pass: all coefficients in the log domain, the
+# frame rotation, the 4x4 right-hand side) and a tau-pass evaluation (k_I
+# only: |p|, the helical direction, |n' x u|, two log2, one rsqrt, two exp2)
 CENSUS_FP32_INSTR = 116
-CENSUS_MUFU = 14
+CENSUS_MUFU = 12
+CENSUS_TAU_FP32_INSTR = 55
+CENSUS_TAU_MUFU = 5
+# DRAM bytes (read + write) of one transfer launch: the ncu capture of the
+# 256x512 render (206 368 items, 6.12 MB read + 6.9 KB written: the hit list
+# and request records; the output planes stay in the 129 MB L2 during the
+# launch) scaled by the full render's 4.004x hit rays
+TRAFFIC_BYTES_PER_LAUNCH = int(round((6123264 + 6912) * 826336 / 206368))
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 256x512 capture "
+                  "(profiles/transfer_persistent_mixed_conical_256x512.md) scaled by the hit rays")
 
 
 def parse():
@@ -401,16 +413,28 @@ def main():
 
     # ---- roofline of the dominant kernel (persistent transfer)
     peaks = ctx.device_peaks()
-    evals_per_s = st_b["rhs_evals"] / (t_step * 1e-3)
-    achieved = evals_per_s * CENSUS_FP32_INSTR * 2 / 1e12
+    # tau-pass evaluations of a render: the same request with the IQUV pass
+    # switched off (tau_min above every depth; the tau pass is unchanged)
+    _, st_tau = ctx.render(model, pdesc, nu, J.make_params(precision="mixed", schedule="persistent",
+                                                           **dict(kw, tau_min=1e300)))
+    n_tau = min(st_tau["rhs_evals"], st_b["rhs_evals"])
+    n_iquv = st_b["rhs_evals"] - n_tau
+    sec = t_step * 1e-3
+    evals_per_s = st_b["rhs_evals"] / sec
+    fp32_instr = n_tau * CENSUS_TAU_FP32_INSTR + n_iquv * CENSUS_FP32_INSTR
+    mufu_ops = n_tau * CENSUS_TAU_MUFU + n_iquv * CENSUS_MUFU
+    achieved = fp32_instr * 2 / sec / 1e12
     roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
-            "frac": achieved / peaks["fp32_tflops"], "traffic": None,
+            "frac": achieved / peaks["fp32_tflops"], "traffic": TRAFFIC_BYTES_PER_LAUNCH,
+            "traffic_source": TRAFFIC_SOURCE,
             "peak_source": "measured FMA-chain microbenchmark on this GPU in this run (MEASURED_PEAKS.json "
                            "holds only HBM and bf16 peaks)",
-            "census": {"fp32_instr_per_rhs": CENSUS_FP32_INSTR, "mufu_per_rhs": CENSUS_MUFU},
+            "census": {"fp32_instr_per_rhs": CENSUS_FP32_INSTR, "mufu_per_rhs": CENSUS_MUFU,
+                       "fp32_instr_per_tau_rhs": CENSUS_TAU_FP32_INSTR, "mufu_per_tau_rhs": CENSUS_TAU_MUFU,
+                       "tau_evals_per_step": int(n_tau), "iquv_evals_per_step": int(n_iquv)},
             "rhs_evals_per_s": evals_per_s,
-            "mufu": {"achieved_tops": evals_per_s * CENSUS_MUFU / 1e12, "peak_tops": peaks["mufu_tops"],
-                     "frac": evals_per_s * CENSUS_MUFU / 1e12 / peaks["mufu_tops"]},
+            "mufu": {"achieved_tops": mufu_ops / sec / 1e12, "peak_tops": peaks["mufu_tops"],
+                     "frac": mufu_ops / sec / 1e12 / peaks["mufu_tops"]},
             "fp64_peak_tflops": peaks["fp64_tflops"]}
     cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 and conical else None
     serving = serving_leg(ctx, args.serve_requests) if args.serve_requests > 0 else None
