@@ -371,6 +371,11 @@ int jsh_grid_interpolate(jsh_ctx* ctx, int32_t grid_id, int32_t field,
 #define JSH_MAX_HULLS 16
 int jsh_hull_upload(jsh_ctx* ctx, const double* zr, int64_t n, int32_t n_circle,
                     int32_t* hull_id);
+/* The profile jsh_hull_upload stores, computed on the host only (no device,
+ * no context): the vertices (vz[i], vR[i]), i = 0..*m, of R(z); vz and vR
+ * must hold n entries.  Same argument checks as jsh_hull_upload. */
+int jsh_hull_profile(const double* zr, int64_t n, int32_t n_circle, double* vz,
+                     double* vR, int32_t* m);
 
 /* --------------------------------------------------------- serving */
 typedef struct jsh_server jsh_server;

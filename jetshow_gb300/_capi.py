@@ -251,6 +251,7 @@ SIGNATURES = [
     ("jsh_grid_interpolate", C.c_int,
      [C.c_void_p, C.c_int32, C.c_int32, _D, C.c_int64, C.c_double, _D]),
     ("jsh_hull_upload", C.c_int, [C.c_void_p, _D, C.c_int64, C.c_int32, _P(C.c_int32)]),
+    ("jsh_hull_profile", C.c_int, [_D, C.c_int64, C.c_int32, _D, _D, _P(C.c_int32)]),
     ("jsh_server_create", C.c_int, [C.c_void_p, _P(ServerConfig), _P(C.c_void_p)]),
     ("jsh_server_destroy", None, [C.c_void_p]),
     ("jsh_server_submit", C.c_int,

@@ -154,6 +154,21 @@ extern "C" int jsh_hull_upload(jsh_ctx* ctx, const double* zr, int64_t n, int32_
   return JSH_OK;
 }
 
+extern "C" int jsh_hull_profile(const double* zr, int64_t n, int32_t n_circle, double* vz, double* vR,
+                                int32_t* m) {
+  if (!zr || !vz || !vR || !m) {
+    jsh_set_error("null argument");
+    return JSH_ERR_INVALID;
+  }
+  HullHost H;
+  int st = build_profile(zr, n, n_circle, &H);
+  if (st) return st;
+  *m = (int32_t)(H.vz.size() - 1);
+  std::copy(H.vz.begin(), H.vz.end(), vz);
+  std::copy(H.vR.begin(), H.vR.end(), vR);
+  return JSH_OK;
+}
+
 int jsh_resolve_hull(jsh_ctx* ctx, JshModel* model) {
   if (model->geo_kind != JSH_GEO_SIMULATION) return JSH_OK;
   if (!ctx) {

@@ -122,3 +122,32 @@ def test_hull_rejects_bad_input(oracle):
         oracle.hull_register(HULL_ID, np.array([[1.0, -0.1], [2.0, 0.2]]), 36)  # r < 0
     with pytest.raises(RuntimeError):
         oracle.hull_register(HULL_ID, np.array([[1.0, 0.1], [2.0, 0.2]]), 2)  # n_circle < 3
+
+
+def product_profile(lib, zr, n_circle=36):
+    import ctypes as C
+    from jetshow_gb300 import _capi as A
+    zr = np.ascontiguousarray(zr, dtype=np.float64)
+    vz = np.zeros(zr.shape[0]); vr = np.zeros(zr.shape[0]); m = C.c_int32()
+    st = lib.jsh_hull_profile(A.dptr(zr), zr.shape[0], n_circle, A.dptr(vz), A.dptr(vr), C.byref(m))
+    return st, vz[:m.value + 1], vr[:m.value + 1]
+
+
+@pytest.mark.parametrize("name", ["rectangle", "parabolic", "cloud"])
+def test_product_profile_equals_oracle(lib, oracle, name):
+    """The library's host profile (what jsh_hull_upload puts on the device)
+    is bitwise the oracle's, so device and oracle clip against the same
+    half-planes."""
+    zr = profiles()[name]
+    st, vz, vr = product_profile(lib, zr)
+    assert st == 0
+    oracle.hull_register(HULL_ID, zr, 36)
+    oz, orr = oracle.hull_profile(HULL_ID)
+    assert np.array_equal(vz, oz) and np.array_equal(vr, orr)
+
+
+def test_product_profile_rejects_bad_input(lib):
+    assert product_profile(lib, np.array([[1.0, 0.1], [1.0, 0.2]]))[0] != 0
+    assert product_profile(lib, np.array([[1.0, -0.1], [2.0, 0.2]]))[0] != 0
+    assert product_profile(lib, np.array([[1.0, 0.1], [2.0, 0.2]]), n_circle=2)[0] != 0
+
