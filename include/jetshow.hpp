@@ -26,6 +26,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -436,6 +437,24 @@ class Observation {
   std::vector<double> tau_, l_, I_, Q_, U_, V_;
   std::vector<uint32_t> status_;
 };
+
+// Text writers of the legacy drivers (src/utils.cpp:211-236): every value
+// divided by `scale`, separated by a space, one image row per line
+// (write_2dvector) or one value per line (write_vector), default ostream
+// formatting.
+inline std::ostream& write_2dvector(std::ostream& os, const std::vector<std::vector<double>>& v,
+                                    double scale = 1.0) {
+  for (const auto& row : v) {
+    for (double x : row) os << x / scale << " ";
+    os << "\n";
+  }
+  return os;
+}
+
+inline std::ostream& write_vector(std::ostream& os, const std::vector<double>& v, double scale = 1.0) {
+  for (double x : v) os << x / scale << " " << "\n";
+  return os;
+}
 
 }  // namespace jetshow
 
