@@ -19,15 +19,18 @@
     }                                                                                   \
   } while (0)
 
+// A slot's `used` flag is set (release) only after its view is complete, so
+// renders that read slots without the context lock (jsh_prepare_request on
+// a serving thread) never see a half-written view.
 struct JshGridSlot {
-  bool used = false;
+  std::atomic<bool> used{false};
   JshGrid view{};
   void* mem = nullptr;  // one allocation holding every array of the grid
   size_t bytes = 0;
 };
 
 struct JshHullSlot {
-  bool used = false;
+  std::atomic<bool> used{false};
   JshHull view{};
   void* mem = nullptr;  // one allocation holding the profile arrays
   size_t bytes = 0;

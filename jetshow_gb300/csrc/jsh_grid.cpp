@@ -455,7 +455,6 @@ extern "C" int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n, const 
     return JSH_ERR_CUDA;
   }
   JshGridSlot& S = ctx->grids[id];
-  S.used = true;
   S.mem = mem;
   S.bytes = total;
   JshGrid& G = S.view;
@@ -476,6 +475,7 @@ extern "C" int jsh_grid_upload(jsh_ctx* ctx, const double* xy, int64_t n, const 
   G.x0f = (float)x0;
   G.y0f = (float)y0;
   G.inv_hf = (float)(1.0 / h);
+  S.used.store(true, std::memory_order_release);
   *grid_id = id;
   return JSH_OK;
 }

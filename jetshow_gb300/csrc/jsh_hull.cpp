@@ -138,7 +138,6 @@ extern "C" int jsh_hull_upload(jsh_ctx* ctx, const double* zr, int64_t n, int32_
     return JSH_ERR_CUDA;
   }
   JshHullSlot& S = ctx->hulls[id];
-  S.used = true;
   S.mem = mem;
   S.bytes = total;
   JshHull& V = S.view;
@@ -150,6 +149,7 @@ extern "C" int jsh_hull_upload(jsh_ctx* ctx, const double* zr, int64_t n, int32_
   V.n_circle = n_circle;
   V.z_min = H.z_min;
   V.z_max = H.z_max;
+  S.used.store(true, std::memory_order_release);
   *hull_id = id;
   return JSH_OK;
 }
