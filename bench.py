@@ -81,6 +81,24 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(value: float, world: int, device="cuda") -> float:
+    """The largest of every rank's value (the slowest replica sets the
+    whole job's time); the value itself on one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: int, world: int, ms_per_step_max: float) -> float:
+    """Whole-job throughput of replicas: the units all ranks processed in one
+    step over the slowest rank's step time."""
+    return units_per_rank * world / (ms_per_step_max * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region."""
 
@@ -370,11 +388,8 @@ def main():
     barrier()
     items = st_b["n_work_items"]
     out_b = {k: v.cpu().numpy() for k, v in planes.items()}
-    t_step = float(np.mean(ms_b))
-    if world > 1:
-        tt = torch.tensor([max(ms_b)], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-    value = items * world / (t_step * 1e-3)
+    t_step = max_over_ranks(float(np.mean(ms_b)), world)
+    value = job_rate(items, world, t_step)
 
     # ---- static mixed and plain FP64 forms
     ms_m, st_m = timed(p_mixed, min(args.steps, 3), 1)
@@ -407,7 +422,7 @@ def main():
         assert rc == 0, ctx.lib.jsh_last_error()
         if i >= args.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
-    e2e_value = st.n_work_items * world / (np.mean(e2e_ms) * 1e-3)
+    e2e_value = job_rate(st.n_work_items, world, max_over_ranks(float(np.mean(e2e_ms)), world))
     d2h = sum(v.numel() * v.element_size() for v in host.values())
     h2d = C.sizeof(A.ModelDesc) + C.sizeof(A.PlaneDesc) + C.sizeof(A.Params) + nu_c.nbytes
 
