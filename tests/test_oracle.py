@@ -151,3 +151,69 @@ def test_scalar_field_polarisation_is_zero(oracle):
     ri = oracle.render(jet.desc(), plane, [15e9], J.make_params(output="I"))
     assert np.all(r["Q"] == 0) and np.all(r["U"] == 0) and np.all(r["V"] == 0)
     assert np.array_equal(r["I"], ri["I"])
+
+
+def _rays_through(n, seed, extent_pc, los):
+    """Image-plane-like rays (direction (-sin los, 0, -cos los)) with
+    origins spread over the jet's neighbourhood."""
+    rng = np.random.default_rng(seed)
+    o = np.column_stack([np.zeros(n), rng.uniform(-0.2, 0.2, n) * extent_pc,
+                         rng.uniform(0.0, 1.0, n) * extent_pc]) * J.pc
+    d = np.tile([-math.sin(los), 0.0, -math.cos(los)], (n, 1))
+    return o, d
+
+
+def test_hit_points_lie_on_the_surfaces(oracle):
+    """Known answer of the geometry: finite chord end points satisfy their
+    surface's quadric to 1e-12 relative -- the cone (d.(p-o))^2 = cos^2(a)
+    |p-o|^2 (src/Cone.cpp:56-118), the cylinder |w|^2 = r/pc in pc units
+    (the reference's c0, src/Cylinder.cpp:53) and the paraboloid x^2 + y^2 =
+    (r0^2/pc) z (src/Geometry.cpp:28-69)."""
+    field = (J.ConstFlatVField(10.0), J.RandomScalarBFieldZ(0.1, 1.0), J.BKNFieldZ(500, 2, True))
+    alpha = 0.05
+    cases = {
+        "cone": (J.Cone((0, 0, 0), (0, 0, 1), alpha, 100 * J.pc),
+                 lambda p: ((p[:, 2] ** 2 - math.cos(alpha) ** 2 * np.sum(p ** 2, axis=1))
+                            / np.sum(p ** 2, axis=1))),
+        "cylinder": (J.Cylinder((0, 0, 0), (0, 0, 1), 0.5 * J.pc),
+                     lambda p: ((p[:, 0] ** 2 + p[:, 1] ** 2) / J.pc ** 2 - 0.5 * J.pc / J.pc) / (0.5 * J.pc / J.pc)),
+        "paraboloid": (J.Parabaloid((0, 0, 0), (0, 0, 1), 0.1 * J.pc, 100 * J.pc),
+                       lambda p: ((p[:, 0] ** 2 + p[:, 1] ** 2 - (0.1 * J.pc) ** 2 / J.pc * p[:, 2])
+                                  / (p[:, 0] ** 2 + p[:, 1] ** 2))),
+    }
+    for name, (geo, residual) in cases.items():
+        o, d = _rays_through(4000, 1, 20.0, 0.1)
+        nseg, seg, st = oracle.hit_rays(J.Jet(geo, *field).desc(), o, d)
+        fin = nseg == 1
+        # chords shorter than the 100 pc (half-)infinite paths are finite on both ends
+        fin &= np.linalg.norm(seg[:, 0, 1] - seg[:, 0, 0], axis=1) < 50 * J.pc
+        assert fin.sum() > 200, name
+        for end in (0, 1):
+            r = residual(seg[fin, 0, end])
+            assert np.max(np.abs(r)) < 1e-12, (name, end, np.max(np.abs(r)))
+
+
+def test_optically_thin_limit(oracle):
+    """Known answer of the transfer: with a density so low that tau ~ 1e-9,
+    I equals the path integral of eta_I to that order."""
+    jet = J.Jet(J.Cone((0, 0, 0), (0, 0, 1), 0.05, 100 * J.pc), J.ConstFlatVField(10.0),
+                J.HelicalConicalBField(0.1, 1.0, math.pi / 4, True), J.BKNField(5e-6, 2.0, True), s=2.5,
+                gamma_min=10.0)
+    m = jet.desc()
+    lg = math.log10(0.4 * 1.8443 * J.pc)
+    plane = J.ImagePlane((8, 8), lg, lg, 0.1).desc()
+    nu = np.array([15.4e9 * 1.1])
+    p = J.make_params(tau_atol=1e-30, tau_rtol=1e-12, atol=1e-40, rtol=1e-11, output="I", tau_max=1e30,
+                      tau_min=1e-300)
+    r = oracle.render(m, plane, nu, p)
+    o, d, _ = oracle.plane_rays(plane)
+    nseg, seg, _ = oracle.hit_rays(m, o, np.tile(d, (o.shape[0], 1)))
+    hit = np.nonzero(nseg == 1)[0]
+    assert hit.size > 4
+    assert np.max(r["tau"][0][hit]) < 1e-6
+    for pix in hit[:3]:
+        a, b = seg[pix, 0, 0], seg[pix, 0, 1]
+        s = np.linspace(0.0, 1.0, 100001)
+        eta = np.array([oracle.coefficients(m, a + t * (b - a), -d, nu[0])[7] for t in s])
+        integral = np.trapezoid(eta, s) * np.linalg.norm(b - a)
+        assert abs(r["I"][0][pix] - integral) / integral < 1e-6, (pix, r["I"][0][pix], integral)
