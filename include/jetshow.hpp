@@ -413,6 +413,23 @@ class Observation {
       for (size_t j = 0; j < sz.second; ++j) img[i][j] = (*src)[off + i * sz.second + j];
     return img;
   }
+  // Observation::run_stripe (src/Observation.cpp:310-347): tau only, along
+  // half of the central row, n constant RK4 steps per intersection, stop at
+  // tau_max; tau_min is accepted and unused, as in the reference.
+  void run_stripe(int n, double tau_max, double tau_min, size_t freq_index = 0) {
+    (void)tau_min;
+    if (freq_index >= nus_.size()) throw std::runtime_error("run_stripe: frequency index out of range");
+    const auto sz = plane_->image_size();
+    stripe_.assign(sz.second - sz.second / 2, 0.0);
+    check(jsh_observation_run_stripe(default_context(), &jet_->desc(), &plane_->desc(), nus_[freq_index], n,
+                                     tau_max, stripe_.data()));
+  }
+  // Image::getStripe (src/Image.cpp:31-41); stripe mode computes tau only.
+  std::vector<double> getStripe(std::string value) const {
+    if (value != "tau") throw std::runtime_error("getStripe: stripe mode computes tau only");
+    if (stripe_.empty()) throw std::runtime_error("getStripe: run_stripe() first");
+    return stripe_;
+  }
   std::pair<unsigned long int, unsigned long int> getImageSize() const { return plane_->image_size(); }
   const jsh_stats& stats() const { return stats_; }
   const std::vector<uint32_t>& status() const { return status_; }
@@ -434,7 +451,7 @@ class Observation {
   std::vector<double> nus_;
   jsh_params params_{};
   jsh_stats stats_{};
-  std::vector<double> tau_, l_, I_, Q_, U_, V_;
+  std::vector<double> tau_, l_, I_, Q_, U_, V_, stripe_;
   std::vector<uint32_t> status_;
 };
 

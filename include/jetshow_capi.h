@@ -10,6 +10,8 @@
  * a message retrievable with jsh_last_error().
  *
  * Reference interfaces replaced (paths inside the jetshow project):
+ *   - Observation::run_stripe / getStripe
+ *       src/Observation.cpp:310-347, src/Image.cpp:31-41 -> jsh_observation_run_stripe
  *   - Observation::run / observe_single_pixel / getImage
  *       src/Observation.cpp:20-41, src/Observation.cpp:349-395,
  *       include/Observation.h:12-24                -> jsh_observation_run
@@ -305,6 +307,16 @@ int jsh_last_stats(jsh_ctx* ctx, jsh_stats* stats);
 int jsh_observation_run_noalloc(const jsh_model_desc* model, const jsh_plane_desc* plane, const double* nu_hz,
                                 int32_t n_nu, const jsh_params* params, void* cuda_stream,
                                 jsh_image* device_out);
+
+/* Stripe mode (Observation::run_stripe + getStripe, src/Observation.cpp:310-347,
+ * src/Image.cpp:31-41): tau only, for the pixels of row n_across/2 from
+ * column n_along/2 to the end, in FP64 on the device with the reference's
+ * integrate_tau (src/Observation.cpp:55-123): n constant RK4 steps per
+ * intersection, stopped at the first step whose tau >= tau_max.
+ * tau_host[n_along - n_along/2] (host buffer); nu_hz source-frame. */
+int jsh_observation_run_stripe(jsh_ctx* ctx, const jsh_model_desc* model,
+                               const jsh_plane_desc* plane, double nu_hz, int32_t n,
+                               double tau_max, double* tau_host);
 
 /* Ray generation on the device (ImagePlane + Image + Ray ctors): origins
  * [n_across*n_along][3], the common unit direction [3], pixel sizes

@@ -239,6 +239,8 @@ SIGNATURES = [
     ("jsh_last_stats", C.c_int, [C.c_void_p, _P(Stats)]),
     ("jsh_observation_run_noalloc", C.c_int,
      [_P(ModelDesc), _P(PlaneDesc), _D, C.c_int32, _P(Params), C.c_void_p, _P(DeviceImage)]),
+    ("jsh_observation_run_stripe", C.c_int,
+     [C.c_void_p, _P(ModelDesc), _P(PlaneDesc), C.c_double, C.c_int32, C.c_double, _D]),
     ("jsh_plane_rays", C.c_int, [C.c_void_p, _P(PlaneDesc), _D, _D, _D]),
     ("jsh_trace_plane", C.c_int,
      [C.c_void_p, _P(ModelDesc), _P(PlaneDesc), _P(C.c_int32), _D, _P(C.c_uint32)]),

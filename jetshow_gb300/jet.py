@@ -406,6 +406,22 @@ class Observation:
                                                                      self.nu, p)
         return self
 
+    def run_stripe(self, n, tau_max, tau_min=0.0, *, freq_index: int = 0, ctx=None):
+        """Observation::run_stripe (src/Observation.cpp:310-347): tau only,
+        along half of the central row, constant-step RK4 (``tau_min`` is
+        accepted and unused, as in the reference)."""
+        self._stripe = (ctx or default_context()).stripe(self.jet.desc(), self.imagePlane.desc(),
+                                                         float(self.nu[freq_index]), n, tau_max)
+        return self
+
+    def getStripe(self, value: str = "tau"):
+        """Image::getStripe (src/Image.cpp:31-41); stripe mode computes tau only."""
+        if getattr(self, "_stripe", None) is None:
+            raise RuntimeError("run_stripe() first")
+        if value != "tau":
+            raise ValueError("stripe mode computes tau only")
+        return self._stripe
+
     def getImage(self, value: str, freq_index: int = 0):
         """[n_across][n_along] plane of "tau", "I", "Q", "U", "V" or "l"."""
         if self._images is None:

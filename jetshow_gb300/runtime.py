@@ -131,6 +131,14 @@ class Context:
                                                  C.byref(gid)))
         return gid.value
 
+    def stripe(self, model: A.ModelDesc, plane: A.PlaneDesc, nu: float, n: int = 100, tau_max: float = 1e4):
+        """tau along half of the central row (Observation::run_stripe +
+        getStripe) on the device: n_along - n_along // 2 values."""
+        out = np.zeros(int(plane.n_along - plane.n_along // 2))
+        check(self.lib, self.lib.jsh_observation_run_stripe(self.handle, C.byref(model), C.byref(plane), float(nu),
+                                                            int(n), float(tau_max), A.dptr(out)))
+        return out
+
     def hull_upload(self, zr, n_circle: int = 36) -> int:
         """Build and upload the hull of SimulationGeometry: the (z, r) points
         [pc] revolved at n_circle azimuths; returns the hull id."""

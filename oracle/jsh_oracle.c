@@ -1438,6 +1438,69 @@ int jo_render(const jsh_model_desc* model, const jsh_plane_desc* plane, const do
 }
 
 /* ====================================================================
+ * Stripe mode: Observation::run_stripe (src/Observation.cpp:310-347) with
+ * integrate_tau (src/Observation.cpp:55-123) and Image::getStripe
+ * (src/Image.cpp:31-41).  Tau only, for the pixels of row n_across / 2 from
+ * column n_along / 2 to the end; per intersection a constant-step
+ * classical RK4 (odeint runge_kutta4) over the const-step time range
+ * [0, L] with dt = L / n, stopped at the first yielded state with tau >=
+ * tau_max (that state's tau is kept and later intersections are dropped);
+ * otherwise the state after the last step.  odeint's const-step iterator
+ * steps while (t + dt) - L <= DBL_EPSILON with t = step * dt.  Pixels whose
+ * ray misses keep tau = 0.
+ * ==================================================================== */
+static double stripe_ray(const model_t* m, v3 ro, v3 rd, double nu, int n, double tau_max) {
+  hits_t h;
+  geo_hit(&m->geo, ro, rd, &h);
+  v3 nl = vmul(rd, -1.);
+  double bg = 0.0;
+  for (int sidx = 0; sidx < h.n; ++sidx) {
+    v3 pin = h.s[sidx].in, pout = h.s[sidx].out;
+    double length = vnorm(vsub(pout, pin));
+    double dt = length / n;
+    tctx_t T = {m, pin, rd, nl, nu, 0};
+    double x = 0.0, t = 0.0, k1, k2, k4, dum = 0.0;
+    int64_t step = 0;
+    int found = (x >= tau_max);
+    if (dt > 0.0) {
+      const double w1 = (1.0 / 6.0) * dt, w2 = (1.0 / 3.0) * dt;
+      while (!found && (t + dt) - length <= DBL_EPSILON && step <= (int64_t)n + 1) {
+        rhs_tau(&T, t, &dum, &k1);
+        rhs_tau(&T, t + 0.5 * dt, &dum, &k2); /* k3 = k2: dtau/dt does not depend on tau */
+        rhs_tau(&T, t + dt, &dum, &k4);
+        x = (((x + w1 * k1) + w2 * k2) + w2 * k2) + w1 * k4;
+        ++step;
+        t = (double)step * dt;
+        found = (x >= tau_max);
+      }
+    }
+    bg += x;
+    if (found) break;
+  }
+  return bg;
+}
+
+int jo_stripe(const jsh_model_desc* model, const jsh_plane_desc* plane, double nu, int32_t n, double tau_max,
+              double* tau_out) {
+  if (!model || !plane || !tau_out || n < 1 || !(nu > 0)) return JSH_ERR_INVALID;
+  model_t m;
+  int st = model_init(model, &m);
+  if (st) return st;
+  plane_t p;
+  st = plane_build(plane, &p);
+  if (st) return st;
+  const uint64_t row = p.n_across / 2, c0 = p.n_along / 2;
+  const int64_t count = (int64_t)(p.n_along - c0);
+#pragma omp parallel for schedule(dynamic)
+  for (int64_t i = 0; i < count; ++i) {
+    v3 ro = plane_origin(&p, row, c0 + (uint64_t)i);
+    tau_out[i] = stripe_ray(&m, ro, p.dir, nu, n, tau_max);
+  }
+  plane_free(&p);
+  return JSH_OK;
+}
+
+/* ====================================================================
  * Integrator known-answer hooks.
  * ==================================================================== */
 typedef struct { double a, b; } lin_t;

@@ -80,6 +80,12 @@ int jo_grid_register(int32_t grid_id, const double* xy, int64_t n,
 double jo_grid_value(int32_t grid_id, int32_t field, double z_pc, double r_pc,
                      double nan_value);
 
+/* Stripe mode (Observation::run_stripe + getStripe): tau of the pixels of
+ * row n_across/2, columns n_along/2 .. n_along-1, constant-step RK4 with
+ * n steps per intersection, stop at tau_max.  tau_out[n_along - n_along/2]. */
+int jo_stripe(const jsh_model_desc* model, const jsh_plane_desc* plane, double nu, int32_t n,
+              double tau_max, double* tau_out);
+
 /* Register the hull of SimulationGeometry under hull_id (0..15): the (z, r)
  * points zr[n][2] in pc revolved at n_circle azimuths. */
 int jo_hull_register(int32_t hull_id, const double* zr, int64_t n, int32_t n_circle);

@@ -64,6 +64,7 @@ def lib():
                                        P(C.c_int32), C.c_int64]
         L.jo_grid_value.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double]
         L.jo_grid_value.restype = C.c_double
+        L.jo_stripe.argtypes = [P(A.ModelDesc), P(A.PlaneDesc), C.c_double, C.c_int32, C.c_double, D]
         L.jo_hull_register.argtypes = [C.c_int32, D, C.c_int64, C.c_int32]
         L.jo_hull_profile.argtypes = [C.c_int32, D, D, P(C.c_int32)]
         L.jo_openmp_threads.restype = C.c_int
@@ -152,6 +153,13 @@ def grid_register(grid_id, xy, values, tri):
 
 def grid_value(grid_id, field, z_pc, r_pc, nan_value=0.0):
     return lib().jo_grid_value(grid_id, field, z_pc, r_pc, nan_value)
+
+
+def stripe(model: A.ModelDesc, plane: A.PlaneDesc, nu: float, n: int = 100, tau_max: float = 1e4):
+    """tau along half of the central row (Observation::run_stripe)."""
+    out = np.zeros(int(plane.n_along - plane.n_along // 2))
+    _chk(lib().jo_stripe(C.byref(model), C.byref(plane), float(nu), int(n), float(tau_max), A.dptr(out)))
+    return out
 
 
 def hull_register(hull_id, zr, n_circle=36):
