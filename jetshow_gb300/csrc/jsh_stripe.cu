@@ -14,10 +14,9 @@
 // evaluation.  A ray that misses keeps tau = 0.
 #include <cuda_runtime.h>
 #include <float.h>
-#include <string.h>
 
+#include <cmath>
 #include <mutex>
-#include <vector>
 
 #include "jsh_context.h"
 #include "jsh_geometry.cuh"
