@@ -53,8 +53,8 @@ CENSUS_TAU_MUFU = 5
 # and request records; the output planes stay in the 129 MB L2 during the
 # launch) scaled by the full render's 4.004x hit rays
 TRAFFIC_BYTES_PER_LAUNCH = int(round((6123264 + 6912) * 826336 / 206368))
-TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 256x512 capture "
-                  "(profiles/transfer_persistent_mixed_conical_256x512.md) scaled by the hit rays")
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one transfer launch on the 256x512 "
+                  "render (206 368 items), scaled by the hit rays")
 
 
 def parse():
