@@ -288,19 +288,22 @@ int jsh_observation_run_device(jsh_ctx* ctx, const jsh_model_desc* model,
 int jsh_last_stats(jsh_ctx* ctx, jsh_stats* stats);
 
 /* Allocation-free form of jsh_observation_run_device, for callers that must
- * not allocate device memory: code running while a stream is captured
- * (cudaMalloc is illegal there), hosts whose framework owns the device
- * memory pool, loops that cannot take cudaMalloc's implicit device
- * synchronisation.  No context: it renders on the current device, enqueued
- * on `cuda_stream`, into the caller's DEVICE output planes, and calls no
- * cudaMalloc, cudaFree or other allocating routine.  Its scratch is one
- * 8 MiB file-scope device array that every GPU loading the library holds
- * until exit; it limits a call to JSH_NOALLOC_MAX_PIXELS pixels,
- * JSH_NOALLOC_MAX_ALONG columns, JSH_NOALLOC_MAX_NU frequencies and analytic
- * (non-gridded) fields, and rejects larger requests with JSH_ERR_INVALID.
- * Calls share the array: calls that overlap on the GPU race.  The first
- * call on a device looks up the array's address; make it before any stream
- * capture.  No counterpart in the reference, which renders on the CPU. */
+ * not allocate device memory: hosts whose framework owns the whole device
+ * memory pool and forbids side allocations, and latency-bound loops that
+ * cannot take the implicit device synchronisation of cudaMalloc/cudaFree.
+ * No context: it renders on the current device, enqueued on `cuda_stream`,
+ * into the caller's DEVICE output planes, and calls no cudaMalloc, cudaFree
+ * or other allocating routine.  The host inputs travel as kernel parameters
+ * (nothing reads the caller's host memory after the call returns).  Its
+ * scratch is one 8 MiB file-scope device array that every GPU loading the
+ * library holds until exit; it limits a call to JSH_NOALLOC_MAX_PIXELS
+ * pixels, JSH_NOALLOC_MAX_ALONG columns, JSH_NOALLOC_MAX_NU frequencies and
+ * analytic fields and geometries (no grids, no hulls), and rejects larger
+ * requests with JSH_ERR_INVALID.  Calls share the array and it keeps the
+ * last call's contents: each call clears what must start at zero, and calls
+ * that overlap on the GPU race.  The first call on a device looks up the
+ * array's address; make it before any stream capture.  No counterpart in
+ * the reference, which renders on the CPU. */
 #define JSH_NOALLOC_MAX_PIXELS 65536
 #define JSH_NOALLOC_MAX_ALONG 4096
 #define JSH_NOALLOC_MAX_NU 64

@@ -23,8 +23,12 @@ to their files by write_2dvector, Stokes maps in Jy (divided by 1e-23 /
 (pixel_size_mas * mas_to_rad)^2, src/utils.cpp:239-245) and lengths in pc.
 Builder choices where the reference API has moved on since the driver: the
 field classes' in_plasma_frame flag (absent in the driver's constructors) is
-True, and the config's tolerances are passed to the integrator (the driver
-left the hard-coded ones).
+True, the config's tolerances are passed to the integrator (the driver
+left the hard-coded ones), and the tau-pass step limit is dl_max_pc * pc cm:
+the driver handed dt_max = pc * dl_max_pc to Observation::run, which
+multiplies by pc once more (src/Observation.cpp:23), so its limit was
+pc^2 * dl_max_pc cm -- in effect none.  Map files of configs whose
+dl_max_pc binds can therefore differ from the legacy driver's.
 """
 from __future__ import annotations
 

@@ -117,7 +117,10 @@ void jsh_bind_request(JshRequest* req, char* base, const JshRequestLayout& L, bo
 }
 
 JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params) {
-  JshLaunchShape s = ctx->shape;
+  return jsh_params_shape(ctx->shape, params);
+}
+
+JshLaunchShape jsh_params_shape(JshLaunchShape s, const jsh_params* params) {
   if (params->block_size > 0) s.block_size = params->block_size;
   if (params->ctas_per_sm > 0) s.ctas_per_sm = params->ctas_per_sm;
   if (params->refill_threshold > 0) s.refill_threshold = params->refill_threshold;

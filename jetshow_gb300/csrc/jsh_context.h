@@ -81,6 +81,10 @@ int jsh_alloc_device(jsh_ctx* ctx, size_t bytes, void** p);
 int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc_host);
 void jsh_free_device(jsh_ctx* ctx, void* p, size_t bytes);
 JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params);
+// The launch knobs of `params` (block size, CTAs per SM, refill threshold,
+// register-capped build) applied over the default shape `s`, clamped to the
+// ranges the launchers accept; needs no context.
+JshLaunchShape jsh_params_shape(JshLaunchShape s, const jsh_params* params);
 // Grow the context workspace to `need` bytes (waits for its previous user).
 int ensure_workspace(jsh_ctx* ctx, size_t need);
 // Enqueue one request on `stream` in the context workspace; dev_out NULL

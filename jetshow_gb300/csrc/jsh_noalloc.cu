@@ -3,23 +3,29 @@
 // work queue, image-plane tables, frequency constants) in one file-scope
 // __device__ array instead of memory from cudaMalloc.
 //
-// Some callers cannot allocate device memory: code that runs while a stream
-// is being captured (cudaMalloc is not a stream operation and is illegal
-// there), hosts whose framework owns the whole device memory pool and
-// forbids side allocations, and latency-bound loops that cannot afford the
-// implicit device synchronisation of cudaMalloc/cudaFree.  They pass their
-// own device output planes and a stream; this entry point allocates nothing
-// (no cudaMalloc, cudaFree, cudaMallocHost or allocating library routine).
+// Some callers cannot allocate device memory: hosts whose framework owns the
+// whole device memory pool and forbids side allocations (a fitting service
+// that hands the renderer slices of its own pool), and latency-bound loops
+// that cannot take the implicit device synchronisation of cudaMalloc /
+// cudaFree.  They pass their own device output planes and a stream; this
+// entry point allocates nothing (no cudaMalloc, cudaFree, cudaMallocHost or
+// allocating library routine).
+//
+// The host-side inputs (the compiled request record, the frequencies and the
+// mixed-precision frequency constants) travel as the parameters of one small
+// staging kernel, which writes them into the array on the caller's stream
+// and clears the counters, hit count, work queue and ranking buckets that
+// must start at zero; nothing reads the caller's host memory after the call
+// returns.
 //
 // The array is sized for at most JSH_NOALLOC_MAX_PIXELS pixels,
 // JSH_NOALLOC_MAX_ALONG columns and JSH_NOALLOC_MAX_NU frequencies; every
 // GPU that loads the library holds it (8 MiB) until the process exits.  All
 // calls share it and it keeps the last call's contents, so calls whose work
-// overlaps on the GPU (different streams, or another process thread) race;
-// the counters, hit count and queue that must start at zero are cleared by
-// each call on its stream.  The first call on a device looks up the array's
-// device address (cudaGetSymbolAddress) with that device current; make that
-// first call before any stream capture.
+// overlaps on the GPU (different streams, or another host thread) race.  The
+// first call on a device looks up the array's device address
+// (cudaGetSymbolAddress) with that device current; make that first call
+// before any stream capture.
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -38,6 +44,33 @@ namespace {
 std::mutex g_setup_mu;
 void* g_scratch_addr[JSH_NOALLOC_MAX_DEVICES] = {nullptr};
 int g_num_sms[JSH_NOALLOC_MAX_DEVICES] = {0};
+
+// Host inputs of one call, passed by value to the staging kernel.
+struct NoallocInputs {
+  JshRequest req;
+  double nu[JSH_NOALLOC_MAX_NU];
+  JshFreqConst fc[JSH_NOALLOC_MAX_NU];
+};
+static_assert(sizeof(NoallocInputs) < 32000, "kernel parameter space");
+
+// One CTA: copies the request record, the frequencies and their constants
+// into the scratch array and zeroes [zero, zero + zero_bytes) (8-byte words).
+__global__ void __launch_bounds__(256) noalloc_stage_kernel(const NoallocInputs in, int n_nu, JshRequest* d_req,
+                                                            double* d_nu, JshFreqConst* d_fc, bool mixed,
+                                                            unsigned long long* zero, unsigned zero_words) {
+  const unsigned t = threadIdx.x;
+  {
+    const unsigned long long* src = (const unsigned long long*)&in.req;
+    unsigned long long* dst = (unsigned long long*)d_req;
+    for (unsigned i = t; i < sizeof(JshRequest) / 8; i += blockDim.x) dst[i] = src[i];
+  }
+  for (int i = (int)t; i < n_nu; i += (int)blockDim.x) {
+    d_nu[i] = in.nu[i];
+    if (mixed) d_fc[i] = in.fc[i];
+  }
+  for (unsigned i = t; i < zero_words; i += blockDim.x) zero[i] = 0ull;
+}
+static_assert(sizeof(JshRequest) % 8 == 0, "request record copied in 8-byte words");
 
 // Device address of the scratch array and the SM count of the current
 // device, looked up once per device.
@@ -89,8 +122,9 @@ extern "C" int jsh_observation_run_noalloc(const jsh_model_desc* model, const js
                   JSH_NOALLOC_MAX_ALONG);
     return JSH_ERR_INVALID;
   }
-  if (uses_grid(model)) {
-    jsh_set_error("gridded fields live in a context; the no-alloc entry point renders analytic models only");
+  if (uses_grid(model) || model->geometry.kind == JSH_GEO_SIMULATION) {
+    jsh_set_error("gridded fields and simulation hulls live in a context; the no-alloc entry point renders "
+                  "analytic models only");
     return JSH_ERR_INVALID;
   }
   for (int i = 0; i < n_nu; ++i) {
@@ -110,9 +144,10 @@ extern "C" int jsh_observation_run_noalloc(const jsh_model_desc* model, const js
   int st = setup_device(dev, &base, &sms);
   if (st) return st;
 
-  JshRequest req;
+  NoallocInputs in;
+  memset(&in, 0, sizeof(in));
   uint64_t np = 0;
-  st = jsh_prepare_request(nullptr, model, plane, params, n_nu, &req, &np);
+  st = jsh_prepare_request(nullptr, model, plane, params, n_nu, &in.req, &np);
   if (st) return st;
   JshRequestLayout L;
   jsh_request_layout(npix, plane->n_along, plane->n_across, n_nu, false, &L);
@@ -121,36 +156,33 @@ extern "C" int jsh_observation_run_noalloc(const jsh_model_desc* model, const js
                   JSH_NOALLOC_SCRATCH_BYTES);
     return JSH_ERR_INVALID;
   }
-  jsh_bind_request(&req, base, L, false);
-  req.tau = device_out->tau;
-  req.l = device_out->l;
-  req.I = device_out->I;
-  req.Q = device_out->Q;
-  req.U = device_out->U;
-  req.V = device_out->V;
-  req.status = device_out->status;
-  JshFreqConst fc[JSH_NOALLOC_MAX_NU];
-  if (params->precision == JSH_PREC_MIXED) {
-    st = jsh_prepare_mixed(&req, nu_hz, fc);
+  jsh_bind_request(&in.req, base, L, false);
+  in.req.tau = device_out->tau;
+  in.req.l = device_out->l;
+  in.req.I = device_out->I;
+  in.req.Q = device_out->Q;
+  in.req.U = device_out->U;
+  in.req.V = device_out->V;
+  in.req.status = device_out->status;
+  const bool mixed = params->precision == JSH_PREC_MIXED;
+  if (mixed) {
+    st = jsh_prepare_mixed(&in.req, nu_hz, in.fc);
     if (st) return st;
   }
+  memcpy(in.nu, nu_hz, sizeof(double) * n_nu);
   cudaStream_t s = (cudaStream_t)cuda_stream;
-  // host sources are pageable locals: cudaMemcpyAsync stages them before returning
-  JSH_CUDA_TRY(cudaMemcpyAsync(base + L.off_req, &req, sizeof(JshRequest), cudaMemcpyHostToDevice, s));
-  JSH_CUDA_TRY(cudaMemcpyAsync(base + L.off_nu, nu_hz, sizeof(double) * n_nu, cudaMemcpyHostToDevice, s));
-  if (params->precision == JSH_PREC_MIXED)
-    JSH_CUDA_TRY(
-        cudaMemcpyAsync(base + L.off_fc, fc, sizeof(JshFreqConst) * n_nu, cudaMemcpyHostToDevice, s));
-  // counters, hit count and work queue start at zero on every call
-  JSH_CUDA_TRY(cudaMemsetAsync(base + L.off_counters, 0, L.off_nu - L.off_counters, s));
+  // counters, hit count, work queue and ranking buckets start at zero on
+  // every call (they lie between off_counters and off_nu)
+  noalloc_stage_kernel<<<1, 256, 0, s>>>(in, n_nu, (JshRequest*)(base + L.off_req), (double*)(base + L.off_nu),
+                                         (JshFreqConst*)(base + L.off_fc), mixed,
+                                         (unsigned long long*)(base + L.off_counters),
+                                         (unsigned)((L.off_nu - L.off_counters) / 8));
+  JSH_CUDA_TRY(cudaGetLastError());
   const JshRequest* d_req = (const JshRequest*)(base + L.off_req);
   JSH_CUDA_TRY(jsh_launch_plane(d_req, 1, plane->n_along, s));
   JSH_CUDA_TRY(jsh_launch_hit(d_req, 1, npix, s));
-  JshLaunchShape shape{params->block_size > 0 ? params->block_size : 128,
-                       params->ctas_per_sm, params->refill_threshold > 0 ? params->refill_threshold : 8};
-  shape.block_size = shape.block_size < 32 ? 32 : (shape.block_size > 256 ? 256 : shape.block_size / 32 * 32);
-  JSH_CUDA_TRY(jsh_launch_transfer(d_req, 1, params->precision, params->schedule,
-                                   params->output == JSH_OUT_FULL, npix * (uint64_t)n_nu, npix, shape,
-                                   (unsigned int*)(base + L.off_queue), sms, s));
+  const JshLaunchShape shape = jsh_params_shape(JshLaunchShape{128, 0, 8, 0}, params);
+  JSH_CUDA_TRY(jsh_launch_transfer(d_req, 1, params->precision, params->schedule, params->output == JSH_OUT_FULL,
+                                   npix * (uint64_t)n_nu, npix, shape, (unsigned int*)(base + L.off_queue), sms, s));
   return JSH_OK;
 }

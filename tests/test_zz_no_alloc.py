@@ -1,12 +1,14 @@
 """The allocation-free entry point (jsh_observation_run_noalloc) against the
 stream-ordered entry point that allocates (jsh_observation_run_device).
 
-Callers inside stream capture, or whose framework owns the device memory,
-cannot call cudaMalloc; this entry point keeps its scratch in a file-scope
-device array.  Two calls in a row must each reproduce the allocating entry
-point's images within the parity tolerances (the array keeps the previous
-call's contents, so the second call checks that everything that must start
-at zero is cleared).  Runs alone in a fresh process or after the suite.
+Callers whose framework owns the device memory pool, or whose loops cannot
+take cudaMalloc's implicit synchronisation, cannot allocate; this entry point
+keeps its scratch in a file-scope device array.  Both entry points run the
+same kernels with the same launch shape, so two calls in a row must each
+reproduce the allocating entry point's images bit for bit (the array keeps
+the previous call's contents, so the second call checks that everything that
+must start at zero is cleared).  Runs alone in a fresh process or after the
+suite.
 """
 import ctypes as C
 
@@ -16,7 +18,6 @@ import pytest
 from jetshow_gb300 import _capi as A
 from jetshow_gb300 import jet as J
 from jetshow_gb300 import workloads as W
-from helpers import compare_images
 
 pytestmark = pytest.mark.gpu
 
@@ -36,14 +37,14 @@ def to_host(t):
     return out
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_noalloc_matches_allocating_entry_point(lib, precision):
+@pytest.mark.parametrize("precision,flags", [("mixed", 0), ("mixed", A.FLAG_COMPACT_REGS), ("fp64", 0)])
+def test_noalloc_matches_allocating_entry_point(lib, precision, flags):
     torch = pytest.importorskip("torch")
     from jetshow_gb300.runtime import Context, check
 
     jet, plane, nu, _ = W.conical_c0(scale=4)
     model, pdesc = jet.desc(), plane.desc()
-    params = J.make_params(precision=precision, schedule="persistent", **W.ACCURATE_KW)
+    params = J.make_params(precision=precision, schedule="persistent", flags=flags, **W.ACCURATE_KW)
     nu = np.ascontiguousarray(nu, dtype=np.float64)
     npix = int(pdesc.n_across * pdesc.n_along)
     stream = torch.cuda.Stream()
@@ -63,8 +64,8 @@ def test_noalloc_matches_allocating_entry_point(lib, precision):
                                                    C.byref(out_img)))
         stream.synchronize()
         got = to_host(out_t)
-        assert np.array_equal(got["status"], ref["status"]), f"call {call}: status differs"
-        compare_images(got, ref, full=True, tau_max=params.tau_max)
+        for k in ("status",) + PLANES:
+            assert np.array_equal(got[k], ref[k]), f"call {call}: plane {k} differs"
     ctx.close()
 
 
