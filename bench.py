@@ -9,11 +9,16 @@ Forms timed in the same run:
   * batched  -- mixed precision (FP32 stages / FP64 tau, Faraday angle and
                 step control), persistent refilling schedule: `value`;
   * mixed    -- the same arithmetic, one thread per item (static schedule);
+  * batched from tau_max -- the batched form integrating IQUV from tau_max
+                like the reference (no optically thick start);
   * plain    -- all-FP64, one thread per item (the plain GPU drop-in).
 `e2e` times the batched form through the C ABI with host buffers (outputs
-copied back to pinned host memory each step).  `--impl reference` times
-the CPU oracle (FP64 restatement of the reference's Observation::run with
-OpenMP over pixels) on a bounded sample of the same workload.
+copied back to pinned host memory each step).  Further legs: the 128x128
+conical jet (C0), the 1024x1024 ParabaloidCone with a Faraday-thick core
+(C2), the simulation-grid jet (C3) and the replayed serving stream (C4).
+`--impl reference` times the CPU oracle (FP64 restatement of the
+reference's Observation::run with OpenMP over pixels) on bounded samples of
+the same workload; it never loads the CUDA library.
 """
 from __future__ import annotations
 
@@ -72,8 +77,12 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-gridded", dest="gridded", action="store_false",
                     help="skip the simulation-grid leg")
-    ap.add_argument("--serve-requests", type=int, default=64,
+    ap.add_argument("--serve-requests", type=int, default=1000,
                     help="requests of the replayed serving stream (0 skips the serving leg)")
+    ap.add_argument("--saturate-rate", type=float, default=5000.0,
+                    help="arrival rate [1/s] of a second replay that saturates the device (0 skips it)")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the C0 and C2 legs")
     return ap.parse_args()
 
 
@@ -144,51 +153,79 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def workload(scale, name="conical", ctx=None):
+def workload(scale, name="conical", ctx=None, pcm=None):
     """The headline workload (the conical jet on the 512x1024 log plane), or
     the simulation-grid jet (its grid triangulated and uploaded to ctx) for
-    profiling that path."""
+    profiling that path.  ``pcm``: parsecs per mas computed by the caller
+    (the reference arm passes the oracle's value)."""
     from jetshow_gb300 import workloads as W
     if name == "simulation-grid":
         from jetshow_gb300.runtime import triangulate
         xy, vals = W.simulation_grid_c3()
         gid = ctx.grid_upload(xy, vals, triangulate(xy))
         return W.simulation_c3(gid, scale=scale)
-    return W.conical_c1(scale=scale)
+    return W.conical_c1(scale=scale, pcm=pcm)
 
 
-def reference_arm(args):
-    """The CPU oracle (OpenMP over pixels, FP64) on a bounded sample."""
+def config_dict(image, n_freq, work_items, world):
+    """The ``config`` of both arms' lines (the same workload, same keys)."""
+    return {"workload": WORKLOAD, "image": list(image), "n_freq": int(n_freq), "work_items": int(work_items),
+            "l2": "GPU arm: 256 MB buffer written between timed steps (the CPU reference arm has no device)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def oracle_hits(O, jet, plane):
+    """Flat indices of the pixels whose ray hits the jet (the oracle's own
+    geometry, bit-exact with the device's)."""
+    o, d, _ = O.plane_rays(plane.desc())
+    nseg, _, _ = O.hit_rays(jet.desc(), o, np.tile(d, (o.shape[0], 1)))
+    return np.nonzero(nseg > 0)[0]
+
+
+def timed_oracle_sample(O, jet, plane, nu, params, hit, rng, n, threads):
+    pix = np.sort(rng.choice(hit, size=min(n, hit.size), replace=False))
+    t0 = time.perf_counter()
+    O.render(jet.desc(), plane.desc(), nu, params, pix=pix, threads=threads)
+    return pix.size * nu.size, time.perf_counter() - t0
+
+
+def reference_arm(args, step_seconds=2.5):
+    """The CPU oracle (OpenMP over pixels on every host core, FP64) on
+    bounded random samples of the headline workload: every step renders a
+    fresh random sample of hit pixels (all four frequencies) sized during
+    the warm-up steps to take about ``step_seconds``.  Only the oracle's
+    library is loaded (no CUDA library, no torch)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    from jetshow_gb300 import _capi as A
     from jetshow_gb300 import jet as J
+    from jetshow_gb300 import workloads as W
     from oracle import oracle as O
     O.build()
-    from jetshow_gb300 import workloads as W
-    jet, plane, nu, _ = workload(args.scale)
+    pcm = O.mas_to_pc(W.Z, A.Cosmology(**W.COSMO_FLAT))
+    jet, plane, nu, _ = workload(args.scale, pcm=pcm)
     params = J.make_params(**W.ACCURATE_KW)
     threads = O.threads()
     rng = np.random.default_rng(0)
-    # hit pixels of the plane (the oracle's own geometry)
-    o, d, _ = O.plane_rays(plane.desc())
-    nseg, _, _ = O.hit_rays(jet.desc(), o, np.tile(d, (o.shape[0], 1)))
-    hit = np.nonzero(nseg > 0)[0]
-    n_sample = min(hit.size, max(64, threads * 16))
-    vals = []
-    for step in range(args.warmup + args.steps):
-        pix = rng.choice(hit, size=n_sample, replace=False)
-        t0 = time.perf_counter()
-        O.render(jet.desc(), plane.desc(), nu, params, pix=pix, threads=threads)
-        dt = time.perf_counter() - t0
-        if step >= args.warmup:
-            vals.append(n_sample * nu.size / dt)
-    v = float(np.mean(vals))
-    sample = f"{n_sample} random hit pixels x {nu.size} freq per step"
+    hit = oracle_hits(O, jet, plane)
+    n = min(hit.size, max(64, threads * 16))
+    vals, items_total, t_total = [], 0, 0.0
+    for step in range(max(args.warmup, 1) + args.steps):
+        items, dt = timed_oracle_sample(O, jet, plane, nu, params, hit, rng, n, threads)
+        if step >= max(args.warmup, 1):
+            vals.append(items / dt)
+            items_total += items
+            t_total += dt
+        else:  # size the sample for about step_seconds per step
+            n = int(min(hit.size, max(16, n * step_seconds / max(dt, 1e-3))))
+    v = items_total / t_total
+    sample = (f"{n} random hit pixels x {nu.size} freq per step (about {step_seconds:.1f} s each), "
+              f"{items_total} items in {t_total:.1f} s over {args.steps} steps")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * n_sample * nu.size / v, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD}, "impl": "reference",
+            "config": config_dict(plane.image_size, nu.size, hit.size * nu.size, args.gpus), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -200,39 +237,40 @@ def cpu_baseline_sample(jet, plane, nu, kw, seconds=10.0):
     O.build()
     params = J.make_params(**kw)
     threads = O.threads()
-    o, d, _ = O.plane_rays(plane.desc())
-    nseg, _, _ = O.hit_rays(jet.desc(), o, np.tile(d, (o.shape[0], 1)))
-    hit = np.nonzero(nseg > 0)[0]
+    hit = oracle_hits(O, jet, plane)
     rng = np.random.default_rng(1)
     n = min(hit.size, max(32, threads * 4))
     total_items, total_t = 0, 0.0
     while total_t < seconds and total_items < hit.size * nu.size:
-        pix = rng.choice(hit, size=n, replace=False)
-        t0 = time.perf_counter()
-        O.render(jet.desc(), plane.desc(), nu, params, pix=pix, threads=threads)
-        total_t += time.perf_counter() - t0
-        total_items += n * nu.size
+        items, dt = timed_oracle_sample(O, jet, plane, nu, params, hit, rng, n, threads)
+        total_t += dt
+        total_items += items
         n = min(hit.size, n * 2)
     return {"value": total_items / total_t, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{total_items} (hit pixel, freq) items drawn at random, {total_t:.1f} s"}
 
 
-def errors_vs_converged(jet, plane, nu, outs, n_pix=2048):
+def errors_vs_converged(jet, plane, nu, outs, n_pix=2048, extra_pix=None):
     """Worst errors of each form against the converged FP64 oracle
-    (rtol 1e-10) on a random sample of hit pixels (every frequency): tau
-    relative (rays below tau_max), I relative where I > 1e-6 max(I) of the
-    sample, Q/U/V over max(I), total flux of the sample."""
+    (rtol 1e-10) on a random sample of hit pixels (every frequency), plus
+    ``extra_pix`` (e.g. the deepest pixels): tau relative (rays below
+    tau_max), I relative where I > 1e-6 max(I) of the sample, Q/U/V over
+    max(I), total flux of the sample."""
     from jetshow_gb300 import jet as J
     from jetshow_gb300 import workloads as W
     from oracle import oracle as O
     O.build()
     ref_status = next(v for v in outs.values() if v is not None)["status"]
     hit = np.nonzero(((ref_status & 1) != 0).any(axis=0))[0]
-    pix = np.sort(np.random.default_rng(7).choice(hit, size=min(n_pix, hit.size), replace=False))
+    pix = np.random.default_rng(7).choice(hit, size=min(n_pix, hit.size), replace=False)
+    if extra_pix is not None:
+        pix = np.concatenate([pix, np.asarray(extra_pix, dtype=np.int64)])
+    pix = np.unique(pix)
     t0 = time.perf_counter()
     ref = O.render(jet.desc(), plane.desc(), nu, J.make_params(**W.CONVERGED_KW), pix=pix, threads=O.threads())
-    res = {"sample": f"{pix.size} random hit pixels x {nu.size} freq, oracle at rtol 1e-10 "
-                     f"({time.perf_counter() - t0:.1f} s)"}
+    res = {"sample": f"{pix.size} hit pixels x {nu.size} freq"
+                     + (f" (incl. the {len(extra_pix)} deepest)" if extra_pix is not None else "")
+                     + f", oracle at rtol 1e-10 ({time.perf_counter() - t0:.1f} s)"}
     for name, out in outs.items():
         if out is None:
             continue
@@ -251,16 +289,39 @@ def errors_vs_converged(jet, plane, nu, outs, n_pix=2048):
     return res
 
 
-def serving_leg(ctx, n_requests):
-    """Replay the seeded Poisson request stream (200 requests/s, priors of
-    the model-fitting sweep) through the serving loop in real time; latency
-    is arrival to result on the host."""
+def faraday_depth(jet, plane, nu_hz, pix, n_pts=4000):
+    """Faraday depth int k_F dl [rad] along the chord(s) of pixel ``pix``
+    with the oracle's lab-frame k_F (src/utils.cpp:77-98 and the thermal
+    term), by the trapezoid rule on points clustered geometrically around
+    the chord's closest approach to the jet apex (k_F ~ r^-3 there)."""
+    from oracle import oracle as O
+    o, d, _ = O.plane_rays(plane.desc())
+    nseg, seg, _ = O.hit_rays(jet.desc(), o[pix:pix + 1], d[None, :])
+    model, nl = jet.desc(), -np.asarray(d)
+    total = 0.0
+    for k in range(int(nseg[0])):
+        a, b = seg[0, k, 0], seg[0, k, 1]
+        L = float(np.linalg.norm(b - a))
+        u = (b - a) / L
+        sc = float(np.clip(-np.dot(a, u), 0.0, L))
+        w = L * np.logspace(-10, 0, n_pts)
+        s = np.unique(np.clip(np.concatenate([[0.0, L, sc], sc - w, sc + w]), 0.0, L))
+        kf = np.array([O.coefficients(model, a + si * u, nl, nu_hz)[4] for si in s])
+        total += float(np.sum(0.5 * (kf[1:] + kf[:-1]) * np.diff(s)))
+    return total
+
+
+def serving_leg(ctx, n_requests, rate_hz=200.0, warm=True):
+    """Replay the seeded Poisson request stream (priors of the model-fitting
+    sweep) through the serving loop in real time; latency is arrival to
+    result on the host."""
     from jetshow_gb300 import serving as S
-    stream = S.request_stream(n_requests, rate_hz=200.0, seed=42)
+    stream = S.request_stream(n_requests, rate_hz=rate_hz, seed=42)
+    counts = {}
     with S.Server(ctx, max_inflight_batches=3, max_batch_requests=16) as srv:
-        # one short stream first: pages in the result path and the host threads
-        S.run_stream(srv, [r for r in S.request_stream(8, rate_hz=200.0, seed=7) if r.size_label == "64x64"])
-        records, wall = S.run_stream(srv, stream)
+        if warm:  # one short stream first: pages in the result path and the host threads
+            S.run_stream(srv, [r for r in S.request_stream(8, rate_hz=200.0, seed=7) if r.size_label == "64x64"])
+        records, wall = S.run_stream(srv, stream, counts=counts)
     lat = np.array([r["latency_ms"] for r in records])
     queue = np.array([r["queue_ms"] for r in records])
     items = sum(r["n_items"] for r in records)
@@ -271,13 +332,13 @@ def serving_leg(ctx, n_requests):
             by_size[label] = {"n": int(sel.sum()), "p50_ms": float(np.percentile(lat[sel], 50)),
                               "p99_ms": float(np.percentile(lat[sel], 99))}
     span = stream[-1].t_arrival
-    return {"requests": len(records), "arrival_rate_hz": 200.0, "wall_s": wall, "arrival_span_s": span,
-            "rays_per_s": items / wall, "offered_rays_per_s": items / span, "work_items": int(items),
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+    return {"requests": len(stream), "completed": len(records), "arrival_rate_hz": rate_hz, "wall_s": wall,
+            "arrival_span_s": span, "rays_per_s": items / wall, "offered_rays_per_s": items / span,
+            "work_items": int(items), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "queue_p50_ms": float(np.percentile(queue, 50)), "queue_p99_ms": float(np.percentile(queue, 99)),
-            "by_size": by_size, "admission_rejections": 0,
+            "by_size": by_size, "admission_rejections": int(counts.get("admission_rejections", 0)),
             "mean_batch_requests": float(np.mean([r["batch_size"] for r in records])),
-            "tolerances": "rtol 1e-6 / 1e-7 tau, atol 1e-24 / 1e-20 tau, mixed precision, full Stokes"}
+            "tolerances": "rtol 1e-6 / 5e-8 tau, atol 1e-24 / 1e-20 tau, mixed precision, full Stokes"}
 
 
 def gridded_leg(ctx, steps=3):
@@ -317,6 +378,73 @@ def gridded_leg(ctx, steps=3):
     return out
 
 
+class Renderer:
+    """Device-timed renders of one workload through jsh_observation_run_device
+    into preallocated device planes (CUDA events on the launching stream, a
+    256 MB buffer written before every step)."""
+
+    def __init__(self, ctx, torch, max_values):
+        self.ctx, self.torch = ctx, torch
+        self.stream = torch.cuda.Stream()
+        self.planes = {k: torch.zeros(max_values, dtype=torch.float64, device="cuda") for k in
+                       ("tau", "l", "I", "Q", "U", "V")}
+        self.planes["status"] = torch.zeros(max_values, dtype=torch.int32, device="cuda")
+        self.ptrs = {k: v.data_ptr() for k, v in self.planes.items()}
+        self.flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(self, model, pdesc, nu, params, steps, warmup):
+        torch = self.torch
+        ms = []
+        for i in range(warmup + steps):
+            self.flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(self.stream):
+                e0.record(self.stream)
+                self.ctx.render_device(model, pdesc, nu, params, self.stream.cuda_stream, self.ptrs)
+                e1.record(self.stream)
+            self.stream.synchronize()
+            if i >= warmup:
+                ms.append(e0.elapsed_time(e1))
+        return ms, self.ctx.last_stats()
+
+    def host(self, n_nu, npix):
+        return {k: v[:n_nu * npix].view(n_nu, npix).cpu().numpy() for k, v in self.planes.items()}
+
+
+def config_leg(R, jet, plane, nu, kw, steps, plain_scale, plain_builder, n_err_pix, n_deep, faraday=False):
+    """One more configuration (C0, C2): the batched form on the full image
+    (device time), the plain all-FP64 form on the same model at
+    ``plain_scale`` (a coarser plane of the same extent: the bounded
+    subset), errors of the batched form against the converged oracle on a
+    random sample plus the ``n_deep`` deepest pixels, and the core Faraday
+    depth at the lowest frequency when asked."""
+    from jetshow_gb300 import jet as J
+    model, pdesc = jet.desc(), plane.desc()
+    npix = plane.image_size[0] * plane.image_size[1]
+    p_b = J.make_params(precision="mixed", schedule="persistent", **kw)
+    ms_b, st_b = R.timed(model, pdesc, nu, p_b, steps, 1)
+    out_b = R.host(nu.size, npix)
+    leg = {"image": list(plane.image_size), "freq_ghz_source": [float(x) / 1e9 for x in nu],
+           "work_items": int(st_b["n_work_items"]), "batched": {
+               "rays_per_s": st_b["n_work_items"] / (np.mean(ms_b) * 1e-3), "ms": float(np.mean(ms_b)),
+               "rhs_evals": int(st_b["rhs_evals"]), "status_or": int(st_b["status_or"])}}
+    jp, plp, nup, _ = plain_builder(plain_scale)
+    ms_p, st_p = R.timed(jp.desc(), plp.desc(), nup, J.make_params(precision="fp64", schedule="static", **kw), 1, 0)
+    leg["plain_fp64"] = {"rays_per_s": st_p["n_work_items"] / (np.mean(ms_p) * 1e-3), "ms": float(np.mean(ms_p)),
+                         "image": list(plp.image_size), "work_items": int(st_p["n_work_items"]),
+                         "subset": f"the same model on a {plp.image_size[0]}x{plp.image_size[1]} plane of the same "
+                                   f"extent"}
+    tau0 = np.where((out_b["status"][0] & 1) != 0, out_b["tau"][0], -1.0)
+    deep = np.argsort(tau0)[::-1][:n_deep]
+    leg["deepest_tau"] = float(tau0[deep[0]])
+    leg["err_vs_converged_oracle"] = errors_vs_converged(jet, plane, nu, {"batched": out_b}, n_pix=n_err_pix,
+                                                         extra_pix=deep)
+    if faraday:
+        leg["core_faraday_depth_rad"] = faraday_depth(jet, plane, float(nu[0]), int(deep[0]))
+    return leg
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -330,6 +458,7 @@ def main():
         dist.init_process_group("nccl")
     from jetshow_gb300 import jet as J
     from jetshow_gb300 import _capi as A
+    from jetshow_gb300 import workloads as W
     from jetshow_gb300.runtime import Context
 
     ctx = Context(local)
@@ -337,34 +466,13 @@ def main():
     model, pdesc = jet.desc(), plane.desc()
     na, nl = plane.image_size
     npix = na * nl
-    stream = torch.cuda.Stream()
-    planes = {k: torch.zeros((nu.size, npix), dtype=torch.float64, device="cuda") for k in
-              ("tau", "l", "I", "Q", "U", "V")}
-    planes["status"] = torch.zeros((nu.size, npix), dtype=torch.int32, device="cuda")
-    ptrs = {k: v.data_ptr() for k, v in planes.items()}
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    R = Renderer(ctx, torch, max(nu.size * npix, 2 * 1024 * 1024))
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def timed(params, steps, warmup):
-        ms = []
-        for i in range(warmup + steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            with torch.cuda.stream(stream):
-                e0.record(stream)
-                ctx.render_device(model, pdesc, nu, params, stream.cuda_stream, ptrs)
-                e1.record(stream)
-            stream.synchronize()
-            if i >= warmup:
-                ms.append(e0.elapsed_time(e1))
-        return ms, ctx.last_stats()
-
-    from jetshow_gb300 import workloads as W
     kw_cfg = dict(kw)
     kw = dict(W.ACCURATE_KW)  # every form at the 1e-4-qualified tolerances
     p_batched = J.make_params(precision="mixed", schedule="persistent", **kw)
@@ -382,27 +490,32 @@ def main():
                   "fixed": True}
     else:
         tuning = ctx.autotune(model, pdesc, nu, p_batched)
+    p_tmax = J.make_params(precision="mixed", schedule="persistent", flags=A.FLAG_IQUV_FROM_TAU_MAX, **kw)
     barrier()
     with ClockSampler(local) as clk:
-        ms_b, st_b = timed(p_batched, args.steps, args.warmup)
+        ms_b, st_b = R.timed(model, pdesc, nu, p_batched, args.steps, args.warmup)
     barrier()
     items = st_b["n_work_items"]
-    out_b = {k: v.cpu().numpy() for k, v in planes.items()}
+    out_b = R.host(nu.size, npix)
     t_step = max_over_ranks(float(np.mean(ms_b)), world)
     value = job_rate(items, world, t_step)
 
-    # ---- static mixed and plain FP64 forms
-    ms_m, st_m = timed(p_mixed, min(args.steps, 3), 1)
+    # ---- static mixed, configuration tolerances, from tau_max, plain FP64
+    ms_m, st_m = R.timed(model, pdesc, nu, p_mixed, min(args.steps, 3), 1)
     mixed_rate = st_m["n_work_items"] / (np.mean(ms_m) * 1e-3)
-    ms_c, st_c = timed(p_cfg, min(args.steps, 3), 1)
+    ms_c, st_c = R.timed(model, pdesc, nu, p_cfg, min(args.steps, 3), 1)
     cfg_rate = st_c["n_work_items"] / (np.mean(ms_c) * 1e-3)
+    ms_t, st_t = R.timed(model, pdesc, nu, p_tmax, min(args.steps, 2), 1)
+    tmax_rate = st_t["n_work_items"] / (np.mean(ms_t) * 1e-3)
+    out_t = R.host(nu.size, npix)
     plain_rate, out_p = None, None
     if not args.no_plain:
-        ms_p, st_p = timed(p_plain, 1, 1)
+        ms_p, st_p = R.timed(model, pdesc, nu, p_plain, 1, 1)
         plain_rate = st_p["n_work_items"] / (np.mean(ms_p) * 1e-3)
-        out_p = {k: v.cpu().numpy() for k, v in planes.items()}
+        out_p = R.host(nu.size, npix)
     conical = args.workload == "conical"
-    rel = errors_vs_converged(jet, plane, nu, {"batched": out_b, "plain": out_p}) if rank == 0 and conical else {}
+    rel = (errors_vs_converged(jet, plane, nu, {"batched": out_b, "batched_from_tau_max": out_t, "plain": out_p})
+           if rank == 0 and conical else {})
 
     # ---- end to end through the C ABI with pinned host buffers
     host = {k: torch.empty((nu.size, npix), dtype=torch.float64, pin_memory=True) for k in
@@ -424,7 +537,7 @@ def main():
             e2e_ms.append((t1 - t0) * 1e3)
     e2e_value = job_rate(st.n_work_items, world, max_over_ranks(float(np.mean(e2e_ms)), world))
     d2h = sum(v.numel() * v.element_size() for v in host.values())
-    h2d = C.sizeof(A.ModelDesc) + C.sizeof(A.PlaneDesc) + C.sizeof(A.Params) + nu_c.nbytes
+    h2d = int(ctx.lib.jsh_request_h2d_bytes(nu_c.size, A.PREC_MIXED))
 
     # ---- roofline of the dominant kernel (persistent transfer)
     peaks = ctx.device_peaks()
@@ -452,27 +565,37 @@ def main():
                      "frac": mufu_ops / sec / 1e12 / peaks["mufu_tops"]},
             "fp64_peak_tflops": peaks["fp64_tflops"]}
     cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 and conical else None
-    serving = serving_leg(ctx, args.serve_requests) if args.serve_requests > 0 else None
+    serving = saturated = None
+    if args.serve_requests > 0:
+        serving = serving_leg(ctx, args.serve_requests)
+        if args.saturate_rate > 0:
+            saturated = serving_leg(ctx, args.serve_requests, rate_hz=args.saturate_rate, warm=False)
     gridded = gridded_leg(ctx) if args.gridded else None
+    configs = None
+    if args.configs and conical and rank == 0:
+        configs = {
+            "C0": config_leg(R, *W.conical_c0()[:3], kw, 10, 1, lambda s: W.conical_c0(scale=s), 1024, 32),
+            "C2": config_leg(R, *W.parabolic_c2()[:3], kw, 2, 32, lambda s: W.parabolic_c2(scale=s), 256, 32,
+                             faraday=True)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "image": [na, nl], "n_freq": int(nu.size),
-                           "work_items": int(items), "l2": "256 MB buffer written between timed steps",
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "config": config_dict((na, nl), nu.size, items, world),
                 "tolerances": {"qualified": {k: W.ACCURATE_KW[k] for k in ("tau_atol", "tau_rtol", "atol", "rtol")},
                                "config": {k: kw_cfg[k] for k in ("tau_atol", "tau_rtol", "atol", "rtol")}},
                 "forms": {"batched_rays_per_s": value, "mixed_static_rays_per_s": mixed_rate,
                           "plain_fp64_rays_per_s": plain_rate,
                           "batched_over_plain": (value / plain_rate) if plain_rate else None,
+                          "batched_from_tau_max_rays_per_s": tmax_rate,
+                          "from_tau_max_over_plain": (tmax_rate / plain_rate) if plain_rate else None,
                           "batched_config_tolerances_rays_per_s": cfg_rate},
                 "err_vs_converged_oracle": rel,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": float(np.mean(e2e_ms))},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
-                "gridded": gridded,
+                "serving_saturated": saturated, "gridded": gridded, "configs": configs,
                 "gpu_launches": int(st_b["kernels_launched"]) * args.steps,
                 "gpu_launches_per_step": {"plane": 2, "hit": 1, "rank": 3, "transfer": 1},
                 "autotuned_shape": tuning, "rhs_evals_per_step": st_b["rhs_evals"],

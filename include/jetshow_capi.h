@@ -35,6 +35,8 @@
  *                                                      JSH_GEO_SIMULATION
  *   - comoving_transfer_distance2 / mas_to_pc
  *       src/utils.cpp:186-208                       -> jsh_mas_to_pc
+ *   - JetModelZoom.ft + FINUFFT_NUNU.forward (type-3 NUFFT of the image)
+ *       jetmodel.py:114-132, fourier.py:40-94        -> jsh_observation_visibilities
  *
  * Units follow the reference: lengths in cm, magnetic field in G, densities
  * in cm^-3, frequencies in Hz, angles in rad.  Images are row-major
@@ -224,6 +226,16 @@ typedef struct jsh_params {
  * Results are bitwise those of the default build; jsh_autotune chooses
  * between the two for requests that leave the launch knobs at 0. */
 #define JSH_FLAG_COMPACT_REGS 0x4
+/* Mixed persistent schedule: run each item's tau pass and I/IQUV pass in one
+ * persistent kernel, whose warps mix lanes of both passes, instead of the
+ * default split (a tau kernel over every item, then an IQUV kernel over the
+ * items that need the second pass, ranked by the optical depth it crosses).
+ * Results are bitwise the same; the flag exists for comparison. */
+#define JSH_FLAG_SINGLE_KERNEL 0x8
+/* Split form: launch the tau kernel's build bounded to 85 registers (24
+ * resident warps per SM, a few spills) instead of the 128-register one.
+ * Results are bitwise the same. */
+#define JSH_FLAG_TAU_DENSE 0x10
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,
@@ -310,6 +322,35 @@ int jsh_last_stats(jsh_ctx* ctx, jsh_stats* stats);
 int jsh_observation_run_noalloc(const jsh_model_desc* model, const jsh_plane_desc* plane, const double* nu_hz,
                                 int32_t n_nu, const jsh_params* params, void* cuda_stream,
                                 jsh_image* device_out);
+
+/* ------------------------------------------------------- visibilities */
+/* The visibility step after the render (JetModelZoom.ft, jetmodel.py:114-132,
+ * with FINUFFT_NUNU's type-3 transform, fourier.py:40-94): for every
+ * frequency f and (u, v) point k,
+ *   V = exp(-2 pi i (u dx + v dy)) sum_j F_j exp(-2 pi i (u' x_j + v' y_j)),
+ *   (u', v') = (u cos rot + v sin rot, -u sin rot + v cos rot),
+ * over the image's pixel centres x_j = -across_j rad_per_cm,
+ * y_j = along_j rad_per_cm and flux densities F_j = I_j size_j^2 jy_per_cgs
+ * (size_j the pixel side in cm).  get_i_image's Jy conversion
+ * (src/pyjetshow.cpp:111-169) is jy_per_cgs = 1e23 (1+z)^-3
+ * (mas_to_rad / (pc_in_mas pc))^2; rad_per_cm = 1 / D_A. */
+typedef struct jsh_vis_desc {
+  double rad_per_cm;  /* angle of 1 cm at the source [rad/cm] (> 0)            */
+  double jy_per_cgs;  /* flux density per (I [cgs] x pixel area [cm^2])        */
+  double dx, dy;      /* [rad] shift of the model on the sky                   */
+  double rot;         /* [rad] rotation of the (u, v) plane                    */
+} jsh_vis_desc;
+
+/* Render (like jsh_observation_run, with the outputs kept on the device)
+ * and transform the Stokes I image of every frequency: uv[n_nu][n_uv][2]
+ * in wavelengths (host), vis_out[n_nu][n_uv][2] (re, im) in Jy (host).  The
+ * sum is evaluated directly on the device (no gridding approximation;
+ * ~1e-7 relative to an FP64 direct sum).  n_across <= 16384. */
+int jsh_observation_visibilities(jsh_ctx* ctx, const jsh_model_desc* model,
+                                 const jsh_plane_desc* plane, const double* nu_hz,
+                                 int32_t n_nu, const jsh_params* params,
+                                 const jsh_vis_desc* vis, const double* uv,
+                                 int64_t n_uv, double* vis_out, jsh_stats* stats);
 
 /* Stripe mode (Observation::run_stripe + getStripe, src/Observation.cpp:310-347,
  * src/Image.cpp:31-41): tau only, for the pixels of row n_across/2 from
@@ -455,6 +496,13 @@ int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model,
  * (TFLOP/s), each from a dependent-chain microbenchmark over every SM.
  * No reference counterpart (the reference has no device code). */
 int jsh_device_peaks(jsh_ctx* ctx, double* fp32_tflops, double* mufu_tops, double* fp64_tflops);
+
+/* Host-to-device bytes that one jsh_observation_run or
+ * jsh_observation_run_device call copies: the compiled request record, the
+ * n_nu frequencies and, for JSH_PREC_MIXED, their FP32 coefficient
+ * constants.  The descriptors themselves are read on the host.  No device
+ * work; no reference counterpart. */
+uint64_t jsh_request_h2d_bytes(int32_t n_nu, int32_t precision);
 
 #ifdef __cplusplus
 }

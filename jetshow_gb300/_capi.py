@@ -32,6 +32,8 @@ ST_IQUV = 0x100
 FLAG_IQUV_FROM_TAU_MAX = 0x1
 FLAG_COST_MAP = 0x2
 FLAG_COMPACT_REGS = 0x4
+FLAG_SINGLE_KERNEL = 0x8
+FLAG_TAU_DENSE = 0x10
 ST_ERRORS = ST_STEP_LIMIT | ST_FAIL_LIMIT | ST_BISECT_LIMIT | ST_NAN | ST_DT_UNDERFLOW
 
 GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE, GEO_SIMULATION = 1, 2, 3, 4, 5
@@ -222,6 +224,16 @@ class Tuning(C.Structure):
     ]
 
 
+class VisDesc(C.Structure):
+    _fields_ = [
+        ("rad_per_cm", C.c_double),
+        ("jy_per_cgs", C.c_double),
+        ("dx", C.c_double),
+        ("dy", C.c_double),
+        ("rot", C.c_double),
+    ]
+
+
 _P = C.POINTER
 _D = _P(C.c_double)
 
@@ -239,6 +251,9 @@ SIGNATURES = [
     ("jsh_last_stats", C.c_int, [C.c_void_p, _P(Stats)]),
     ("jsh_observation_run_noalloc", C.c_int,
      [_P(ModelDesc), _P(PlaneDesc), _D, C.c_int32, _P(Params), C.c_void_p, _P(DeviceImage)]),
+    ("jsh_observation_visibilities", C.c_int,
+     [C.c_void_p, _P(ModelDesc), _P(PlaneDesc), _D, C.c_int32, _P(Params), _P(VisDesc), _D, C.c_int64, _D,
+      _P(Stats)]),
     ("jsh_observation_run_stripe", C.c_int,
      [C.c_void_p, _P(ModelDesc), _P(PlaneDesc), C.c_double, C.c_int32, C.c_double, _D]),
     ("jsh_plane_rays", C.c_int, [C.c_void_p, _P(PlaneDesc), _D, _D, _D]),
@@ -263,6 +278,7 @@ SIGNATURES = [
      [C.c_void_p, C.c_uint64, C.c_int32, _P(Image), _P(RequestStats)]),
     ("jsh_server_cancel", C.c_int, [C.c_void_p, C.c_uint64]),
     ("jsh_device_peaks", C.c_int, [C.c_void_p, _D, _D, _D]),
+    ("jsh_request_h2d_bytes", C.c_uint64, [C.c_int32, C.c_int32]),
     ("jsh_autotune", C.c_int,
      [C.c_void_p, _P(ModelDesc), _P(PlaneDesc), _D, C.c_int32, _P(Params), _P(Tuning)]),
 ]

@@ -83,7 +83,7 @@ extern "C" int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model, const jsh
   for (bool cp : {false, true}) {
     if (cp && !try_compact) continue;
     for (int bs : {64, 96, 128, 192, 256}) {
-      const int occ = jsh_persistent_occupancy(p.precision, full, bs, cp);
+      const int occ = jsh_persistent_occupancy(p.precision, full, bs, cp, (p.flags & JSH_FLAG_SINGLE_KERNEL) != 0);
       if (occ < 1) continue;
       std::vector<int> per_sm = {occ};
       if (occ > 1) per_sm.push_back(occ - 1);

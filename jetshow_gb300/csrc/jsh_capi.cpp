@@ -69,6 +69,10 @@ void jsh_request_layout(uint64_t npix, uint64_t n_along, uint64_t n_across, int3
   o = align_up(o + sizeof(uint32_t));
   L->off_buckets = o;
   o = align_up(o + sizeof(uint32_t) * JSH_RANK_BUCKETS * 2);
+  L->off_iq_count = o;
+  o = align_up(o + sizeof(uint32_t));
+  L->off_iq_buckets = o;
+  o = align_up(o + sizeof(uint32_t) * JSH_RANK_BUCKETS * 2);
   L->off_nu = o;
   o = align_up(o + sizeof(double) * n_nu);
   L->off_fc = o;
@@ -85,6 +89,10 @@ void jsh_request_layout(uint64_t npix, uint64_t n_along, uint64_t n_across, int3
   o = align_up(o + sizeof(uint32_t) * npix);
   L->off_key = o;
   o = align_up(o + npix);
+  L->off_iq_items = o;
+  o = align_up(o + sizeof(JshIquvItem) * npix * (uint64_t)n_nu);
+  L->off_iq_order = o;
+  o = align_up(o + sizeof(uint32_t) * npix * (uint64_t)n_nu);
   L->own_outputs = own_outputs;
   for (int k = 0; k < 7; ++k) {
     L->off_out[k] = o;
@@ -105,6 +113,10 @@ void jsh_bind_request(JshRequest* req, char* base, const JshRequestLayout& L, bo
   req->buckets = (uint32_t*)(base + L.off_buckets);
   req->order = (uint32_t*)(base + L.off_order);
   req->key = (uint8_t*)(base + L.off_key);
+  req->iq_items = (JshIquvItem*)(base + L.off_iq_items);
+  req->iq_order = (uint32_t*)(base + L.off_iq_order);
+  req->iq_count = (uint32_t*)(base + L.off_iq_count);
+  req->iq_buckets = (uint32_t*)(base + L.off_iq_buckets);
   if (own_outputs) {
     req->tau = (double*)(base + L.off_out[0]);
     req->l = (double*)(base + L.off_out[1]);
@@ -116,6 +128,11 @@ void jsh_bind_request(JshRequest* req, char* base, const JshRequestLayout& L, bo
   }
 }
 
+int jsh_kernels_per_request(int precision, int schedule, bool single) {
+  if (precision == JSH_PREC_MIXED && schedule == JSH_SCHED_PERSISTENT) return single ? 7 : 11;
+  return 4;
+}
+
 JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params) {
   return jsh_params_shape(ctx->shape, params);
 }
@@ -125,6 +142,8 @@ JshLaunchShape jsh_params_shape(JshLaunchShape s, const jsh_params* params) {
   if (params->ctas_per_sm > 0) s.ctas_per_sm = params->ctas_per_sm;
   if (params->refill_threshold > 0) s.refill_threshold = params->refill_threshold;
   if (params->flags & JSH_FLAG_COMPACT_REGS) s.compact = 1;
+  if (params->flags & JSH_FLAG_SINGLE_KERNEL) s.single = 1;
+  if (params->flags & JSH_FLAG_TAU_DENSE) s.tau_dense = 1;
   if (s.block_size < 32) s.block_size = 32;
   if (s.block_size > 512) s.block_size = 512;
   s.block_size = s.block_size / 32 * 32;
@@ -345,8 +364,9 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
                                    ctx->num_sms, stream));
   JSH_CUDA_TRY(cudaEventRecord(ctx->ws_ready, stream));
   ctx->last_pending = true;
-  // plane (2), hit, transfer; the persistent mixed schedule adds 3 ranking kernels
-  ctx->last_kernels = (params->precision == JSH_PREC_MIXED && params->schedule == JSH_SCHED_PERSISTENT) ? 7 : 4;
+  // plane (2), hit, transfer; the persistent mixed schedule adds 3 ranking
+  // kernels, and its split form the tau kernel and 3 IQUV ranking kernels
+  ctx->last_kernels = jsh_kernels_per_request(params->precision, params->schedule, shape.single != 0);
   ctx->last_counters_off = L.off_counters;
   ctx->last_nhit_off = L.off_nhit;
   ctx->last_npix = npix;
@@ -583,4 +603,11 @@ extern "C" int jsh_device_peaks(jsh_ctx* ctx, double* fp32_tflops, double* mufu_
   JSH_CUDA_TRY(cudaSetDevice(ctx->device));
   JSH_CUDA_TRY(jsh_run_peaks(ctx->num_sms, fp32_tflops, mufu_tops, fp64_tflops, ctx->stream));
   return JSH_OK;
+}
+
+extern "C" uint64_t jsh_request_h2d_bytes(int32_t n_nu, int32_t precision) {
+  if (n_nu < 0) n_nu = 0;
+  uint64_t b = sizeof(JshRequest) + sizeof(double) * (uint64_t)n_nu;
+  if (precision == JSH_PREC_MIXED) b += sizeof(JshFreqConst) * (uint64_t)n_nu;
+  return b;
 }

@@ -38,8 +38,9 @@ struct JshHullSlot {
 
 // Layout of one request's device memory inside an arena allocation.
 struct JshRequestLayout {
-  size_t off_req, off_counters, off_nhit, off_queue, off_buckets, off_nu, off_fc, off_along_size, off_along_center,
-      off_across, off_hits, off_order, off_key, off_out[7];
+  size_t off_req, off_counters, off_nhit, off_queue, off_buckets, off_iq_count, off_iq_buckets, off_nu, off_fc,
+      off_along_size, off_along_center, off_across, off_hits, off_order, off_key, off_iq_items, off_iq_order,
+      off_out[7];
   size_t total;
   bool own_outputs;
 };
@@ -85,6 +86,8 @@ JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params)
 // register-capped build) applied over the default shape `s`, clamped to the
 // ranges the launchers accept; needs no context.
 JshLaunchShape jsh_params_shape(JshLaunchShape s, const jsh_params* params);
+// Kernels one request launches (plane, hit, ranking, transfer).
+int jsh_kernels_per_request(int precision, int schedule, bool single);
 // Grow the context workspace to `need` bytes (waits for its previous user).
 int ensure_workspace(jsh_ctx* ctx, size_t need);
 // Enqueue one request on `stream` in the context workspace; dev_out NULL

@@ -28,11 +28,22 @@ __device__ __forceinline__ D3 cross(D3 a, D3 b) {
 
 // ---------------------------------------------------------- gridded field
 // Containing triangle of (px, py) = (z, r) [pc] by the bucket list, then
-// barycentric weights; nan_value outside the hull or on NaN.
+// barycentric weights; nan_value outside the hull or on NaN.  Every
+// operation is an explicitly rounded FP64 intrinsic in a fixed order (no
+// contraction into fma), the order the oracle's plain-C restatement rounds
+// in: the orientation determinants (b - a) x (c - a) as
+// (bx - ax)(cy - ay) - (by - ay)(cx - ax), each weight one division by the
+// triangle's, the value ((w0 v0 + w1 v1) + w2 v2).  With that, the device
+// and the oracle accept the same first triangle of a bucket's ascending list
+// and return the same bits.
+__device__ __forceinline__ double orient2_rn(double ax, double ay, double bx, double by, double cx, double cy) {
+  return __dsub_rn(__dmul_rn(__dsub_rn(bx, ax), __dsub_rn(cy, ay)), __dmul_rn(__dsub_rn(by, ay), __dsub_rn(cx, ax)));
+}
+
 __device__ inline double grid_value(const JshGrid& G, int field, double px, double py, double nan_value) {
   if (G.n_tri == 0) return nan_value;
   if (!(px >= G.x0 && py >= G.y0)) return nan_value;
-  int i = (int)floor((px - G.x0) / G.h), j = (int)floor((py - G.y0) / G.h);
+  int i = (int)floor(__ddiv_rn(__dsub_rn(px, G.x0), G.h)), j = (int)floor(__ddiv_rn(__dsub_rn(py, G.y0), G.h));
   if (i >= G.nbx) i = G.nbx - 1;
   if (j >= G.nby) j = G.nby - 1;
   if (i < 0 || j < 0) return nan_value;
@@ -44,24 +55,28 @@ __device__ inline double grid_value(const JshGrid& G, int field, double px, doub
     double ax = G.xy[2 * v0], ay = G.xy[2 * v0 + 1];
     double bx = G.xy[2 * v1], by = G.xy[2 * v1 + 1];
     double cx = G.xy[2 * v2], cy = G.xy[2 * v2 + 1];
-    double area = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+    double area = orient2_rn(ax, ay, bx, by, cx, cy);
     if (area == 0) continue;
-    double w0 = ((bx - px) * (cy - py) - (by - py) * (cx - px)) / area;
-    double w1 = ((px - ax) * (cy - ay) - (py - ay) * (cx - ax)) / area;
-    double w2 = ((bx - ax) * (py - ay) - (by - ay) * (px - ax)) / area;
+    double w0 = __ddiv_rn(orient2_rn(px, py, bx, by, cx, cy), area);
+    double w1 = __ddiv_rn(orient2_rn(ax, ay, px, py, cx, cy), area);
+    double w2 = __ddiv_rn(orient2_rn(ax, ay, bx, by, px, py), area);
     if (w0 < 0 || w1 < 0 || w2 < 0) continue;
-    double val = w0 * (double)G.val[(int64_t)v0 * G.n_fields + field] +
-                 w1 * (double)G.val[(int64_t)v1 * G.n_fields + field] +
-                 w2 * (double)G.val[(int64_t)v2 * G.n_fields + field];
+    double val = __dadd_rn(__dadd_rn(__dmul_rn(w0, (double)G.val[(int64_t)v0 * G.n_fields + field]),
+                                     __dmul_rn(w1, (double)G.val[(int64_t)v1 * G.n_fields + field])),
+                           __dmul_rn(w2, (double)G.val[(int64_t)v2 * G.n_fields + field]));
     if (isnan(val)) return nan_value;
     return val;
   }
   return nan_value;
 }
 
+// (x, y, z) [cm] -> (z/pc, hypot(x, y)/pc) (src/SimulationInterpolater.cpp:46-50),
+// the cylindrical radius as sqrt(x^2 + y^2) in correctly rounded steps
+// (within an ulp of a libm hypot for these magnitudes; the oracle rounds
+// the same way).
 __device__ __forceinline__ double sim_value(const JshGrid& G, int field, D3 p, double nan_value) {
-  double x = p.x / JSH_PC, y = p.y / JSH_PC, z = p.z / JSH_PC;
-  return grid_value(G, field, z, hypot(x, y), nan_value);
+  double x = __ddiv_rn(p.x, JSH_PC), y = __ddiv_rn(p.y, JSH_PC), z = __ddiv_rn(p.z, JSH_PC);
+  return grid_value(G, field, z, __dsqrt_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y))), nan_value);
 }
 
 // ---------------------------------------------------------------- V

@@ -14,6 +14,8 @@ struct JshLaunchShape {
   int ctas_per_sm;       // persistent schedule: CTAs per SM (0: occupancy max)
   int refill_threshold;  // persistent schedule: refill when >= this many lanes idle
   int compact;           // mixed persistent schedule: the 168-register build (<= 128 threads)
+  int single;            // mixed persistent schedule: tau and IQUV passes in one kernel (else split)
+  int tau_dense;         // split form: the tau kernel's 85-register build (24 warps per SM)
 };
 
 // Ray generation: along sizes and centres (sequential recurrence of
@@ -47,7 +49,8 @@ cudaError_t jsh_launch_plane_rays(const JshPlane& plane, double* d_orig, double*
 cudaError_t jsh_launch_grid_interp(const JshGrid& grid, int field, const double* d_zr, int64_t n,
                                    double nan_value, double* d_out, cudaStream_t stream);
 
-// Largest resident CTAs per SM of the persistent transfer kernel (compact:
-// the register-capped build of the mixed kernel; 0 if it cannot run
+// Largest resident CTAs per SM of the persistent transfer kernel whose launch
+// shape the knobs set (mixed: the IQUV kernel of the split form, or the
+// single-kernel form; compact: its register-capped build; 0 if it cannot run
 // block_size threads).
-int jsh_persistent_occupancy(int precision, bool full, int block_size, bool compact = false);
+int jsh_persistent_occupancy(int precision, bool full, int block_size, bool compact = false, bool single = false);

@@ -43,6 +43,11 @@ namespace jsh {
 namespace {
 
 constexpr uint8_t PH_IDLE = 0, PH_TAU = 1, PH_IQUV = 2;
+// Which passes a lane machine runs: both (the static schedule and the
+// single-kernel persistent form), the tau pass only (the split form's first
+// kernel: an item that needs an I/IQUV pass is handed on as a JshIquvItem),
+// or the I/IQUV pass only (the split form's second kernel).
+constexpr int PASS_BOTH = 0, PASS_TAU = 1, PASS_IQUV = 2;
 // Optical depth of the equilibrium start of full-Stokes IQUV passes.
 // Measured with the oracle's coefficients against the integration from
 // tau_max (scipy Radau at rtol 1e-11) on 27 rays of depth 94 .. 3.2e4 of the
@@ -147,6 +152,7 @@ struct Lane {
   int32_t nsteps, fails;
   uint32_t status;
   uint32_t evals, acc, rej;
+  uint32_t evals0;       // split form, IQUV kernel: the item's tau-pass evaluations (cost map)
 };
 
 // Stage derivatives of this thread: shared[(s * NK + c) * blockDim + tid].
@@ -310,6 +316,77 @@ __device__ __forceinline__ void lane_finish(Lane& L, const JshRequest* __restric
   L.phase = PH_IDLE;
 }
 
+// Split form, IQUV kernel: the item's Stokes planes and final status (its
+// tau and l planes were written by the tau kernel; with the cost map, l is
+// rewritten with the evaluations of both passes).
+__device__ __noinline__ void write_finished_iquv(const JshRequest* __restrict__ reqs, int r, int f, uint32_t h,
+                                                 float chi_hi, float chi_lo, float x0, float x1, float x2,
+                                                 float x3, uint32_t status, uint32_t evals0, uint32_t evals,
+                                                 uint32_t acc, uint32_t rej) {
+  const JshRequest& R = reqs[r];
+  const JshHit& H = R.hits[h];
+  uint64_t q = (uint64_t)f * R.npix + (uint64_t)H.pix;
+  double S = R.mix.fc[f].scale;
+  float sh, ch;
+  sincosf(chi_hi, &sh, &ch);
+  const float ss = fmaf(chi_lo, ch, sh), sc = fmaf(-chi_lo, sh, ch);
+  if (R.l && (R.P.flags & JSH_FLAG_COST_MAP)) R.l[q] = (double)(evals0 + evals);
+  if (R.I) R.I[q] = S * (double)x0;
+  if (R.Q) R.Q[q] = S * (double)fmaf(sc, x1, -ss * x2);
+  if (R.U) R.U[q] = S * (double)fmaf(ss, x1, sc * x2);
+  if (R.V) R.V[q] = S * (double)x3;
+  if (R.status) R.status[q] = status;
+  unsigned long long* c = R.counters;
+  atomicAdd(&c[0], (unsigned long long)evals);
+  atomicAdd(&c[1], (unsigned long long)acc);
+  atomicAdd(&c[2], (unsigned long long)rej);
+  atomicOr(&c[3], (unsigned long long)status);
+}
+
+// Optical depth the I/IQUV pass of an item integrates through (its cost
+// grows with it), bucketed by half octaves; everything below 0.5 in bucket 1.
+__device__ __forceinline__ uint8_t iquv_cost_key(double tau_bg, bool eq, bool first, const JshMixed& X) {
+  double d = eq ? X.tau_eq : (first ? fmin(tau_bg, X.tau_thick) : tau_bg);
+  if (!(d > 0.5)) return 1;
+  const int k = (int)floorf(2.f * __log2f((float)d)) + 3;
+  return (uint8_t)min(max(k, 1), JSH_RANK_BUCKETS - 1);
+}
+
+// Split form, tau kernel: hand an item whose I/IQUV pass is still to run to
+// the IQUV kernel.  Writes the item's tau and l planes and its tau-pass
+// counters, appends its record to the request's list (one atomic per
+// request among the lanes that emit together).
+__device__ __noinline__ void emit_iquv(const JshRequest* __restrict__ reqs, int r, int f, uint32_t h, double tau_bg,
+                                       double thick, double t_first, int first_seg, int nseg, bool eq,
+                                       uint32_t status, uint32_t evals, uint32_t acc, uint32_t rej) {
+  const JshRequest& R = reqs[r];
+  const JshHit& H = R.hits[h];
+  uint64_t q = (uint64_t)f * R.npix + (uint64_t)H.pix;
+  if (R.tau) R.tau[q] = tau_bg;
+  if (R.l) R.l[q] = (R.P.flags & JSH_FLAG_COST_MAP) ? (double)evals : thick;
+  const unsigned mask = __activemask();
+  const unsigned peers = __match_any_sync(mask, r);
+  const int leader = __ffs(peers) - 1;
+  const unsigned lane = threadIdx.x & 31u;
+  uint32_t slot = 0;
+  if ((int)lane == leader) slot = atomicAdd(R.iq_count, (uint32_t)__popc(peers));
+  slot = __shfl_sync(peers, slot, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+  JshIquvItem it;
+  it.h = h;
+  it.f = (uint16_t)f;
+  it.key = iquv_cost_key(tau_bg, eq, first_seg >= 0, R.mix);
+  it.flags = (uint8_t)((nseg & 3) | (eq ? 4 : 0) | ((first_seg + 1) << 3));
+  it.status = status;
+  it.evals = evals;
+  it.tau_bg = tau_bg;
+  it.t_first = t_first;
+  R.iq_items[slot] = it;
+  unsigned long long* c = R.counters;
+  atomicAdd(&c[0], (unsigned long long)evals);
+  atomicAdd(&c[1], (unsigned long long)acc);
+  atomicAdd(&c[2], (unsigned long long)rej);
+}
+
 // Bisection for the tau_max crossing on the dense output of the last step
 // (src/Observation.cpp:166-190); returns the crossing time [pc].
 __device__ __noinline__ double crossing_time(double tau_old, double t_old, double dt_used, float h, float k1,
@@ -408,23 +485,78 @@ __device__ __noinline__ float4 equilibrium_state(const JshRequest* __restrict__ 
   return make_float4((float)x[0], (float)x[1], (float)x[2], (float)x[3]);
 }
 
+__device__ __forceinline__ void lane_finish_iquv(Lane& L, const JshRequest* __restrict__ reqs) {
+  write_finished_iquv(reqs, L.r, L.f, L.h, L.chi.hi, L.chi.lo, L.x[0], L.x[1], L.x[2], L.x[3], L.status, L.evals0,
+                      L.evals, L.acc, L.rej);
+  L.phase = PH_IDLE;
+}
+
+// Split form, IQUV kernel: start work item w (heaviest-first over the
+// batch's emitted items) where the tau kernel left it -- the I/IQUV pass's
+// first segment, start point and state (zero, or the local equilibrium).
+__device__ __forceinline__ void lane_start_iquv(Lane& L, const JshRequest* __restrict__ reqs,
+                                                const unsigned long long* base, int n_req, unsigned long long w) {
+  const int r = find_request(base, n_req, w);
+  const JshRequest& R = reqs[r];
+  const JshIquvItem it = R.iq_items[R.iq_order[w - base[r]]];
+  L.r = r;
+  L.f = it.f;
+  L.h = it.h;
+  L.phase = PH_IQUV;
+  L.nseg = (int8_t)(it.flags & 3);
+  L.first_seg = (int8_t)((it.flags >> 3) & 3) - 1;
+  const bool eq = (it.flags & 4) != 0;
+  L.tau_bg = it.tau_bg;
+  L.thick = 0.0;
+  L.t_first = it.t_first;
+  L.chi = DF{0.f, 0.f};
+  L.x[0] = L.x[1] = L.x[2] = L.x[3] = 0.f;
+  L.status = it.status;
+  L.evals0 = it.evals;
+  L.evals = L.acc = L.rej = 0;
+  L.seg = L.first_seg >= 0 ? L.first_seg : L.nseg - 1;
+  const JshHit& H = R.hits[L.h];
+  if (eq) {
+    const int s = L.seg;
+    const double tc = L.t_first * JSH_PC;
+    const float4 xe = equilibrium_state(reqs, L.r, L.f, H.seg[s][0] + R.plane.rx * tc, H.seg[s][1] + R.plane.ry * tc,
+                                        H.seg[s][2] + R.plane.rz * tc);
+    L.x[0] = xe.x;
+    L.x[1] = xe.y;
+    L.x[2] = xe.z;
+    L.x[3] = xe.w;
+  }
+  begin_iquv_segment(L, R, H);
+}
+
 // FP32 unit roundoff; the Stokes error norm's noise floor is
 // kNoise * h * scale.  The rounding noise of the embedded error estimate of
 // a Stokes component is about 0.3 u h scale (four terms of magnitude
 // <= scale per derivative, weighted by |e_j| <= 0.05).
 constexpr float kNoise = 5.9604645e-8f;
 
+// Stage components of a lane machine: the IQUV state and chi (full Stokes),
+// I only, or tau only (the split form's tau kernel).
+template <bool FULL, int PASS>
+struct StageWidth {
+  static constexpr int NK = (FULL && PASS != PASS_TAU) ? 5 : 1;
+  static constexpr int NX = (FULL && PASS != PASS_TAU) ? 4 : 1;
+};
+
 // One Dormand-Prince attempt (or a phase transition) of an active lane.
 // warp_tau: every active lane of the warp is in its tau pass, so only k_I
-// is evaluated.
-template <bool FULL>
+// is evaluated.  PASS restricts the machine to one pass (PASS_TAU: an item
+// needing an I/IQUV pass is emitted at the transition; PASS_IQUV: lanes
+// start in their IQUV pass); the arithmetic of each pass is the same in
+// every form, so the images are bitwise the same.
+template <bool FULL, int PASS>
 __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict__ reqs, bool warp_tau,
-                                          const Stages<FULL ? 5 : 1>& K) {
-  constexpr int NK = FULL ? 5 : 1;
-  constexpr int NX = FULL ? 4 : 1;
+                                          const Stages<StageWidth<FULL, PASS>::NK>& K) {
+  constexpr int NK = StageWidth<FULL, PASS>::NK;
+  constexpr int NX = StageWidth<FULL, PASS>::NX;
   const JshRequest& R = reqs[L.r];
   const JshFreqConst F = R.mix.fc[L.f];
-  const bool tau = (L.phase == PH_TAU);
+  const bool tau = PASS == PASS_TAU ? true : (PASS == PASS_IQUV ? false : (L.phase == PH_TAU));
   const bool coef_full = FULL && !(tau && warp_tau);
   // integration direction: +d in the tau pass, -d (towards the observer) after
   const F3 nl = f3(R.mix.nl[0], R.mix.nl[1], R.mix.nl[2]);
@@ -662,6 +794,10 @@ segment_done : {
     begin_iquv_segment(L, R, H);
     return;
   }
+  if (PASS == PASS_IQUV) {
+    lane_finish_iquv(L, reqs);
+    return;
+  }
   lane_finish(L, reqs);
   return;
 }
@@ -679,6 +815,12 @@ start_iquv : {
     // eq_min are integrated whole from their far end
     if (L.tau_bg >= R.mix.eq_min || (L.status & JSH_ST_TAU_CROSSED)) eq = true;
     else L.first_seg = -1;
+  }
+  if (PASS == PASS_TAU) {
+    emit_iquv(reqs, L.r, L.f, L.h, L.tau_bg, L.thick, L.t_first, L.first_seg, L.nseg, eq, L.status, L.evals, L.acc,
+              L.rej);
+    L.phase = PH_IDLE;
+    return;
   }
   L.seg = L.first_seg >= 0 ? L.first_seg : L.nseg - 1;
   const JshHit& H = R.hits[L.h];
@@ -700,6 +842,10 @@ abort:
   if (tau) {
     L.tau_bg += df_val(L.tau_seg);
     L.thick += L.length_cm;
+  }
+  if (PASS == PASS_IQUV) {
+    lane_finish_iquv(L, reqs);
+    return;
   }
   lane_finish(L, reqs);
 }
@@ -788,7 +934,7 @@ __global__ void __launch_bounds__(128) transfer_static_mixed_kernel(const JshReq
   const Stages<FULL ? 5 : 1> K{ksh};
   Lane L;
   lane_start(L, reqs, base, n_req, w, false);
-  while (L.phase != PH_IDLE) lane_step<FULL>(L, reqs, L.phase == PH_TAU, K);
+  while (L.phase != PH_IDLE) lane_step<FULL, PASS_BOTH>(L, reqs, L.phase == PH_TAU, K);
 }
 
 // Persistent CTAs: each warp keeps 32 lanes busy, refilling idle lanes from
@@ -830,13 +976,179 @@ __global__ void __launch_bounds__(COMPACT ? 128 : 256, COMPACT ? 3 : 1)
       continue;
     }
     bool warp_tau = __all_sync(0xffffffffu, L.phase != PH_IQUV);
-    if (L.phase != PH_IDLE) lane_step<FULL>(L, reqs, warp_tau, K);
+    if (L.phase != PH_IDLE) lane_step<FULL, PASS_BOTH>(L, reqs, warp_tau, K);
+  }
+}
+
+// ------------------------------------------------------------ split form
+// The persistent schedule's default form runs the passes in two kernels:
+// every item's tau pass first (one stage component, k_I only: a short
+// right-hand side, few registers, many resident warps, and no warp whose
+// lanes mix tau and IQUV code), then the I/IQUV pass of the items that need
+// one, ranked by the optical depth it integrates through.
+
+// Tau kernel: persistent CTAs, lanes refilled from the ranked queue (the
+// same order as the single-kernel form), each item's tau pass to its end.
+// MINB resident 256-thread CTAs per SM bound its registers: 2 (at most 128,
+// no spills) or 3 (at most 85, a few spills, 24 warps per SM).
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) transfer_tau_kernel(const JshRequest* __restrict__ reqs, int n_req,
+                                                              unsigned long long* queue, int refill) {
+  __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
+  extern __shared__ float ksh[];
+  batch_prefix(reqs, n_req, base);
+  const Stages<1> K{ksh};
+  const unsigned long long total = base[n_req];
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  Lane L;
+  L.phase = PH_IDLE;
+  bool exhausted = false;
+  for (;;) {
+    unsigned idle = __ballot_sync(0xffffffffu, L.phase == PH_IDLE);
+    int nidle = __popc(idle);
+    if (!exhausted && (nidle >= refill || nidle == 32) && nidle > 0) {
+      unsigned long long b = 0;
+      if (lane == 0) b = atomicAdd(queue, (unsigned long long)nidle);
+      b = __shfl_sync(0xffffffffu, b, 0);
+      if (b + (unsigned long long)nidle >= total) exhausted = true;
+      if (L.phase == PH_IDLE) {
+        unsigned long long w = b + (unsigned long long)__popc(idle & lt_mask);
+        if (w < total) lane_start(L, reqs, base, n_req, w, true);
+      }
+    }
+    unsigned active = __ballot_sync(0xffffffffu, L.phase != PH_IDLE);
+    if (active == 0) {
+      if (exhausted) break;
+      continue;
+    }
+    if (L.phase != PH_IDLE) lane_step<false, PASS_TAU>(L, reqs, true, K);
+  }
+}
+
+// Cost histogram of the emitted items of request blockIdx.y (grid-stride).
+__global__ void __launch_bounds__(256) iquv_hist_kernel(const JshRequest* __restrict__ reqs) {
+  __shared__ uint32_t hist[JSH_RANK_BUCKETS];
+  const JshRequest& R = reqs[blockIdx.y];
+  for (int b = threadIdx.x; b < JSH_RANK_BUCKETS; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
+  const uint32_t n = *R.iq_count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(&hist[R.iq_items[i].key], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < JSH_RANK_BUCKETS; b += blockDim.x)
+    if (hist[b]) atomicAdd(&R.iq_buckets[b], hist[b]);
+}
+
+// Start of each cost bucket in descending order (one thread per request).
+__global__ void iquv_prefix_kernel(const JshRequest* __restrict__ reqs) {
+  const JshRequest& R = reqs[blockIdx.x];
+  if (threadIdx.x != 0) return;
+  uint32_t run = 0;
+  for (int b = JSH_RANK_BUCKETS - 1; b >= 0; --b) {
+    R.iq_buckets[JSH_RANK_BUCKETS + b] = run;
+    run += R.iq_buckets[b];
+  }
+}
+
+// iq_order[position] = emitted item; lanes with the same bucket take
+// consecutive positions with one atomic.
+__global__ void __launch_bounds__(256) iquv_scatter_kernel(const JshRequest* __restrict__ reqs) {
+  const JshRequest& R = reqs[blockIdx.y];
+  const uint32_t n = *R.iq_count;
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int key = R.iq_items[i].key;
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    const int leader = __ffs(peers) - 1;
+    uint32_t b = 0;
+    if ((int)lane == leader) b = atomicAdd(&R.iq_buckets[JSH_RANK_BUCKETS + key], (uint32_t)__popc(peers));
+    b = __shfl_sync(peers, b, leader);
+    R.iq_order[b + __popc(peers & ((1u << lane) - 1u))] = i;
+  }
+}
+
+// Exclusive prefix of the emitted items over the batch, in shared memory.
+__device__ __forceinline__ void iquv_prefix(const JshRequest* __restrict__ reqs, int n_req,
+                                            unsigned long long* base) {
+  if (threadIdx.x == 0) {
+    unsigned long long acc = 0;
+    for (int r = 0; r < n_req; ++r) {
+      base[r] = acc;
+      acc += (unsigned long long)(*reqs[r].iq_count);
+    }
+    base[n_req] = acc;
+  }
+  __syncthreads();
+}
+
+// IQUV kernel: persistent CTAs over the ranked emitted items (COMPACT: the
+// register-capped build, as for the single-kernel form).
+template <bool FULL, bool COMPACT>
+__global__ void __launch_bounds__(COMPACT ? 128 : 256, COMPACT ? 3 : 1)
+    transfer_iquv_kernel(const JshRequest* __restrict__ reqs, int n_req, unsigned long long* queue, int refill) {
+  __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
+  extern __shared__ float ksh[];
+  iquv_prefix(reqs, n_req, base);
+  const Stages<FULL ? 5 : 1> K{ksh};
+  const unsigned long long total = base[n_req];
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  Lane L;
+  L.phase = PH_IDLE;
+  bool exhausted = false;
+  for (;;) {
+    unsigned idle = __ballot_sync(0xffffffffu, L.phase == PH_IDLE);
+    int nidle = __popc(idle);
+    if (!exhausted && (nidle >= refill || nidle == 32) && nidle > 0) {
+      unsigned long long b = 0;
+      if (lane == 0) b = atomicAdd(queue, (unsigned long long)nidle);
+      b = __shfl_sync(0xffffffffu, b, 0);
+      if (b + (unsigned long long)nidle >= total) exhausted = true;
+      if (L.phase == PH_IDLE) {
+        unsigned long long w = b + (unsigned long long)__popc(idle & lt_mask);
+        if (w < total) lane_start_iquv(L, reqs, base, n_req, w);
+      }
+    }
+    unsigned active = __ballot_sync(0xffffffffu, L.phase != PH_IDLE);
+    if (active == 0) {
+      if (exhausted) break;
+      continue;
+    }
+    if (L.phase != PH_IDLE) lane_step<FULL, PASS_IQUV>(L, reqs, false, K);
   }
 }
 
 template <bool FULL>
 constexpr size_t stage_smem(int block) {
   return sizeof(float) * 7 * (FULL ? 5 : 1) * (size_t)block;
+}
+
+// Resident CTAs per SM of the IQUV kernel / the single-kernel form.
+int occupancy_mixed(bool split, bool full, int block_size, bool compact) {
+  int n = 0;
+  if (compact && block_size > 128) return 0;
+  const size_t sm = full ? stage_smem<true>(block_size) : stage_smem<false>(block_size);
+#define JSH_OCC(kernel) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block_size, sm)
+  if (split) {
+    if (compact) {
+      if (full) JSH_OCC((transfer_iquv_kernel<true, true>));
+      else JSH_OCC((transfer_iquv_kernel<false, true>));
+    } else {
+      if (full) JSH_OCC((transfer_iquv_kernel<true, false>));
+      else JSH_OCC((transfer_iquv_kernel<false, false>));
+    }
+  } else {
+    if (compact) {
+      if (full) JSH_OCC((transfer_persistent_mixed_kernel<true, true>));
+      else JSH_OCC((transfer_persistent_mixed_kernel<false, true>));
+    } else {
+      if (full) JSH_OCC((transfer_persistent_mixed_kernel<true, false>));
+      else JSH_OCC((transfer_persistent_mixed_kernel<false, false>));
+    }
+  }
+#undef JSH_OCC
+  return n;
 }
 
 }  // namespace
@@ -863,56 +1175,62 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
     rank_prefix_kernel<<<n_req, 32, 0, stream>>>(d_reqs);
     rank_scatter_kernel<<<g, 256, 0, stream>>>(d_reqs);
   }
+  unsigned long long* q = (unsigned long long*)queue;  // [0]: tau / single-kernel queue, [1]: IQUV queue
+  const uint64_t need = (max_items + 31) / 32 * 32;
+  const int rf = shape.refill_threshold;
+  const bool split = !shape.single;
+  if (split) {
+    // tau kernel: 256 threads, every CTA it can keep resident
+    const int bt = 256;
+    int per_sm_t = 0;
+    if (shape.tau_dense)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_t, transfer_tau_kernel<3>, bt, stage_smem<false>(bt));
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_t, transfer_tau_kernel<2>, bt, stage_smem<false>(bt));
+    if (per_sm_t < 1) per_sm_t = 1;
+    unsigned bl_t = (unsigned)(num_sms * per_sm_t);
+    if ((uint64_t)bl_t * bt > need) bl_t = (unsigned)((need + bt - 1) / bt);
+    if (bl_t == 0) bl_t = 1;
+    if (shape.tau_dense)
+      transfer_tau_kernel<3><<<bl_t, bt, stage_smem<false>(bt), stream>>>(d_reqs, n_req, q, rf);
+    else
+      transfer_tau_kernel<2><<<bl_t, bt, stage_smem<false>(bt), stream>>>(d_reqs, n_req, q, rf);
+    const dim3 gi((unsigned)num_sms, (unsigned)n_req);
+    iquv_hist_kernel<<<gi, 256, 0, stream>>>(d_reqs);
+    iquv_prefix_kernel<<<n_req, 32, 0, stream>>>(d_reqs);
+    iquv_scatter_kernel<<<gi, 256, 0, stream>>>(d_reqs);
+  }
   int bs = shape.block_size;
   if (bs > (shape.compact ? 128 : 256)) bs = shape.compact ? 128 : 256;
-  int per_sm = shape.ctas_per_sm > 0 ? shape.ctas_per_sm
-                                     : jsh_persistent_occupancy(JSH_PREC_MIXED, full, bs, shape.compact);
+  int per_sm = shape.ctas_per_sm > 0 ? shape.ctas_per_sm : occupancy_mixed(split, full, bs, shape.compact);
   if (per_sm < 1) per_sm = 1;
   unsigned blocks = (unsigned)(num_sms * per_sm);
-  uint64_t need = (max_items + 31) / 32 * 32;
   if ((uint64_t)blocks * bs > need) blocks = (unsigned)((need + bs - 1) / bs);
   if (blocks == 0) blocks = 1;
-  unsigned long long* q = (unsigned long long*)queue;
-  const int rf = shape.refill_threshold;
-  if (shape.compact) {
-    if (full)
-      transfer_persistent_mixed_kernel<true, true><<<blocks, bs, stage_smem<true>(bs), stream>>>(d_reqs, n_req, q, rf);
-    else
-      transfer_persistent_mixed_kernel<false, true><<<blocks, bs, stage_smem<false>(bs), stream>>>(d_reqs, n_req, q,
-                                                                                                 rf);
+  const size_t smem = full ? stage_smem<true>(bs) : stage_smem<false>(bs);
+  if (split) {
+    if (shape.compact) {
+      if (full) transfer_iquv_kernel<true, true><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf);
+      else transfer_iquv_kernel<false, true><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf);
+    } else {
+      if (full) transfer_iquv_kernel<true, false><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf);
+      else transfer_iquv_kernel<false, false><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf);
+    }
+  } else if (shape.compact) {
+    if (full) transfer_persistent_mixed_kernel<true, true><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q, rf);
+    else transfer_persistent_mixed_kernel<false, true><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q, rf);
   } else {
-    if (full)
-      transfer_persistent_mixed_kernel<true, false><<<blocks, bs, stage_smem<true>(bs), stream>>>(d_reqs, n_req, q,
-                                                                                                rf);
-    else
-      transfer_persistent_mixed_kernel<false, false><<<blocks, bs, stage_smem<false>(bs), stream>>>(d_reqs, n_req, q,
-                                                                                                  rf);
+    if (full) transfer_persistent_mixed_kernel<true, false><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q, rf);
+    else transfer_persistent_mixed_kernel<false, false><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q, rf);
   }
   return cudaGetLastError();
 }
 
 int jsh_queue64_occupancy(int block_size);
 
-int jsh_persistent_occupancy(int precision, bool full, int block_size, bool compact) {
-  int n = 0;
-  if (precision == JSH_PREC_MIXED) {
-    if (compact && block_size > 128) return 0;
-    if (compact && full)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<true, true>, block_size,
-                                                    stage_smem<true>(block_size));
-    else if (compact)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<false, true>, block_size,
-                                                    stage_smem<false>(block_size));
-    else if (full)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<true, false>, block_size,
-                                                    stage_smem<true>(block_size));
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transfer_persistent_mixed_kernel<false, false>, block_size,
-                                                    stage_smem<false>(block_size));
-  } else {
-    n = jsh_queue64_occupancy(block_size);
-  }
-  return n;
+int jsh_persistent_occupancy(int precision, bool full, int block_size, bool compact, bool single) {
+  if (precision == JSH_PREC_MIXED) return occupancy_mixed(!single, full, block_size, compact);
+  return jsh_queue64_occupancy(block_size);
 }
 
 // ------------------------------------------------------------------ host

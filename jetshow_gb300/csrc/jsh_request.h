@@ -17,6 +17,21 @@ struct JshHit {           // one intersecting pixel (Intersection list)
 // Cost buckets of the heaviest-first ranking (factors of 2 in optical depth).
 #define JSH_RANK_BUCKETS 64
 
+// Persistent mixed schedule, split form: one work item whose tau pass has
+// finished and whose I/IQUV pass is still to run, as the tau kernel hands it
+// to the IQUV kernel (32 bytes).  The tau and l planes of the item are
+// written already; the IQUV kernel writes I, Q, U, V and the final status.
+struct JshIquvItem {
+  uint32_t h;          // hit index
+  uint16_t f;          // frequency index
+  uint8_t key;         // IQUV cost bucket (heaviest-first order)
+  uint8_t flags;       // bits 0-1: nseg; bit 2: equilibrium start; bits 3-4: first_seg + 1
+  uint32_t status;     // status bits of the tau pass (JSH_ST_IQUV set)
+  uint32_t evals;      // right-hand-side evaluations of the tau pass (cost map)
+  double tau_bg;       // total optical depth of the tau pass
+  double t_first;      // [pc] IQUV start on first_seg (tau_max crossing or optically thick point)
+};
+
 struct JshParamsDev {
   int32_t n, full, precision, schedule, flags, pad_;
   double tau_max, tau_min, dt_max;
@@ -82,6 +97,14 @@ struct JshRequest {
   uint8_t* key;
   uint32_t* buckets;
   uint32_t* n_hit;        // device counter written by the hit kernel
+  // persistent mixed schedule, split form: items handed from the tau kernel
+  // to the IQUV kernel [npix * n_nu], their heaviest-first order, their
+  // count and the cost-bucket counts / cursors [2][JSH_RANK_BUCKETS] (count
+  // and buckets zeroed with the counters)
+  JshIquvItem* iq_items;
+  uint32_t* iq_order;
+  uint32_t* iq_count;
+  uint32_t* iq_buckets;
   const double* nu;       // device [n_nu] source-frame frequencies
   int32_t n_nu;
   int32_t reserved;

@@ -158,11 +158,25 @@ struct jsh_server {
 namespace {
 
 // Counters region of slot s: [JSH_MAX_BATCH][8] u64 counters, n_hit[JSH_MAX_BATCH],
-// [JSH_MAX_BATCH][2][JSH_RANK_BUCKETS] rank buckets, then the queue counter.
+// [JSH_MAX_BATCH][2][JSH_RANK_BUCKETS] rank buckets, the IQUV item counts
+// [JSH_MAX_BATCH] and their [JSH_MAX_BATCH][2][JSH_RANK_BUCKETS] cost
+// buckets, then the queue counters.
 size_t nhit_off() { return align_up(sizeof(unsigned long long) * 8 * JSH_MAX_BATCH); }
 size_t buckets_off() { return nhit_off() + align_up(sizeof(uint32_t) * JSH_MAX_BATCH); }
+size_t iq_count_off() { return buckets_off() + align_up(sizeof(uint32_t) * 2 * JSH_RANK_BUCKETS * JSH_MAX_BATCH); }
+size_t iq_buckets_off() { return iq_count_off() + align_up(sizeof(uint32_t) * JSH_MAX_BATCH); }
 size_t counters_region_bytes() {
-  return buckets_off() + align_up(sizeof(uint32_t) * 2 * JSH_RANK_BUCKETS * JSH_MAX_BATCH) + 256;
+  return iq_buckets_off() + align_up(sizeof(uint32_t) * 2 * JSH_RANK_BUCKETS * JSH_MAX_BATCH) + 256;
+}
+
+// Pointers of record i into the slot's counters region.
+void bind_counters(JshRequest& r, char* ctl, size_t counters_off, int i) {
+  char* c = ctl + counters_off;
+  r.counters = (unsigned long long*)c + 8 * i;
+  r.n_hit = (uint32_t*)(c + nhit_off()) + i;
+  r.buckets = (uint32_t*)(c + buckets_off()) + 2 * JSH_RANK_BUCKETS * i;
+  r.iq_count = (uint32_t*)(c + iq_count_off()) + i;
+  r.iq_buckets = (uint32_t*)(c + iq_buckets_off()) + 2 * JSH_RANK_BUCKETS * i;
 }
 
 int prepare_request(jsh_server* S, Request* q) {
@@ -189,11 +203,7 @@ void bind(jsh_server* S, Slot& sl, Request* q, int i) {
   JshRequest r = q->rec;
   jsh_bind_request(&r, blk, q->L, true);
   char* ctl = sl.dev;
-  unsigned long long* counters = (unsigned long long*)(ctl + sl.counters_off);
-  uint32_t* nhit = (uint32_t*)(ctl + sl.counters_off + nhit_off());
-  r.counters = counters + 8 * i;
-  r.n_hit = nhit + i;
-  r.buckets = (uint32_t*)(ctl + sl.counters_off + buckets_off()) + 2 * JSH_RANK_BUCKETS * i;
+  bind_counters(r, ctl, sl.counters_off, i);
   r.nu = (const double*)(ctl + offsetof(SlotHost, nu) + sizeof(double) * JSH_SERVER_MAX_NU * i);
   r.mix.fc = (const JshFreqConst*)(ctl + offsetof(SlotHost, fc) + sizeof(JshFreqConst) * JSH_SERVER_MAX_NU * i);
   sl.host->recs[i] = r;
@@ -207,12 +217,7 @@ void bind(jsh_server* S, Slot& sl, Request* q, int i) {
 void bind_empty(Slot& sl, int i) {
   JshRequest r;
   memset(&r, 0, sizeof(r));
-  char* ctl = sl.dev;
-  unsigned long long* counters = (unsigned long long*)(ctl + sl.counters_off);
-  uint32_t* nhit = (uint32_t*)(ctl + sl.counters_off + nhit_off());
-  r.counters = counters + 8 * i;
-  r.n_hit = nhit + i;
-  r.buckets = (uint32_t*)(ctl + sl.counters_off + buckets_off()) + 2 * JSH_RANK_BUCKETS * i;
+  bind_counters(r, sl.dev, sl.counters_off, i);
   r.plane.n_across = 2;
   r.plane.n_along = 0;
   sl.host->recs[i] = r;

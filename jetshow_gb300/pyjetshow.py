@@ -75,3 +75,30 @@ def get_iquv_image(los_angle, redshift, number_of_pixels_along, number_of_pixels
                        pixel_size_mas_start, pixel_size_mas_stop, cone_half_angle, B_1, m, K_1, n, Gamma,
                        nu_observed_ghz, tau_max, central_vfield, **kw)
     return (obs.getImage("tau"),) + tuple(obs.getImage(k) / scales for k in ("I", "Q", "U", "V"))
+
+
+MAS_TO_RAD = 4.84813681109536e-09
+
+
+def get_i_visibilities(los_angle, redshift, number_of_pixels_along, number_of_pixels_across, pixel_size_mas_start,
+                       pixel_size_mas_stop, cone_half_angle, B_1, m, K_1, n, Gamma, nu_observed_ghz, uv, dx=0.0,
+                       dy=0.0, rot=0.0, tau_max=10000., central_vfield=False, pc_per_mas_uv=None, ctx=None, **kw):
+    """Visibilities [Jy] of the get_i_image model at ``uv`` [n_uv, 2]
+    (wavelengths), as JetModelZoom.ft computes them: shift by (dx, dy) mas,
+    (u, v) rotated by ``rot``, pixel centres at the image's own coordinates
+    (across with the "d = -pc_y" sign), flux densities in Jy per pixel.
+    ``pc_per_mas_uv`` sets the angular scale of the pixel coordinates (the
+    fitting code takes it from its own cosmology); by default the binding's
+    mas_to_pc(redshift).  Returns complex [n_uv] (one frequency) or
+    [n_nu, n_uv]."""
+    ctx = ctx or default_context()
+    jet, plane, pc_in_mas = _setup(los_angle, redshift, number_of_pixels_along, number_of_pixels_across,
+                                   pixel_size_mas_start, pixel_size_mas_stop, cone_half_angle, B_1, m, K_1, n,
+                                   Gamma, central_vfield)
+    nu = np.atleast_1d(np.asarray(nu_observed_ghz, dtype=np.float64)) * 1E+09 * (1. + redshift)
+    p = J.make_params(n=100, tau_max=tau_max, dt_max=J.pc * 0.001 * J.pc, tau_min=1e-10, output="I", **kw)
+    pcm_uv = pc_in_mas if pc_per_mas_uv is None else float(pc_per_mas_uv)
+    jy = 1e23 / (1. + redshift) ** 3 * (MAS_TO_RAD / (pc_in_mas * J.pc)) ** 2
+    vis, _ = ctx.visibilities(jet.desc(), plane.desc(), nu, p, uv, MAS_TO_RAD / (pcm_uv * J.pc), jy,
+                              dx * MAS_TO_RAD, dy * MAS_TO_RAD, rot)
+    return vis[0] if np.ndim(nu_observed_ghz) == 0 else vis

@@ -69,6 +69,29 @@ class Context:
                                                             A.dptr(nu), nu.size, C.byref(params),
                                                             C.c_void_p(stream_ptr), C.byref(img)))
 
+    def visibilities(self, model: A.ModelDesc, plane: A.PlaneDesc, nu, params: A.Params, uv, rad_per_cm: float,
+                     jy_per_cgs: float, dx: float = 0.0, dy: float = 0.0, rot: float = 0.0):
+        """Render and transform the Stokes I image on the device
+        (jsh_observation_visibilities): ``uv`` [n_uv, 2] wavelengths (the same
+        points for every frequency) or [n_nu, n_uv, 2]; returns complex
+        visibilities [n_nu, n_uv] in Jy and the render's stats."""
+        nu = np.ascontiguousarray(np.atleast_1d(nu), dtype=np.float64)
+        uv = np.asarray(uv, dtype=np.float64)
+        if uv.ndim == 2:
+            uv = np.broadcast_to(uv, (nu.size,) + uv.shape)
+        uv = np.ascontiguousarray(uv)
+        if uv.shape[0] != nu.size or uv.shape[-1] != 2:
+            raise ValueError("uv must be [n_uv, 2] or [n_nu, n_uv, 2]")
+        n_uv = uv.shape[1]
+        out = np.zeros((nu.size, n_uv, 2))
+        vd = A.VisDesc(rad_per_cm=float(rad_per_cm), jy_per_cgs=float(jy_per_cgs), dx=float(dx), dy=float(dy),
+                       rot=float(rot))
+        st = A.Stats()
+        check(self.lib, self.lib.jsh_observation_visibilities(self.handle, C.byref(model), C.byref(plane),
+                                                              A.dptr(nu), nu.size, C.byref(params), C.byref(vd),
+                                                              A.dptr(uv), n_uv, A.dptr(out), C.byref(st)))
+        return out[..., 0] + 1j * out[..., 1], stats_dict(st)
+
     def autotune(self, model: A.ModelDesc, plane: A.PlaneDesc, nu, params: A.Params) -> dict:
         """Search the persistent schedule's launch shape on this request and
         make the fastest the context default (results do not depend on it)."""

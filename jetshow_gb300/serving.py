@@ -129,13 +129,17 @@ def request_stream(n: int, rate_hz: float = 200.0, seed: int = 42) -> list:
     return out
 
 
-def run_stream(server: Server, stream: list, params: A.Params | None = None, keep_results=False):
+def run_stream(server: Server, stream: list, params: A.Params | None = None, keep_results=False,
+               counts: dict | None = None):
     """Replay a request stream in real time: submit each request at its
     arrival time while a collector thread copies every finished result to
     the host as soon as it completes (in completion order).  Returns the
     per-request records (``latency_ms`` = scheduled arrival to result on
     host, so a late submission counts against the server) and the wall time
-    of the whole stream."""
+    of the whole stream.  A request the server refuses at admission (larger
+    than its whole HBM budget: ``JSH_ERR_OOM``) is counted, not raised;
+    ``counts`` (if given) receives ``submitted`` and ``admission_rejections``."""
+    from .runtime import JetshowError
     import threading
 
     params = params or J.make_params(precision=server.precision, schedule="persistent", **ACCURATE_KW)
@@ -176,18 +180,30 @@ def run_stream(server: Server, stream: list, params: A.Params | None = None, kee
                 time.sleep(0.0002)
 
     th = threading.Thread(target=collect, daemon=True)
+    rejected = 0
     t0 = time.perf_counter()
     th.start()
-    for r in stream:
-        now = time.perf_counter() - t0
-        if r.t_arrival > now:
-            time.sleep(r.t_arrival - now)
-        rid = server.submit(r.jet.desc(), r.plane.desc(), r.nu, params)
-        with lock:
-            pending[rid] = r
-    done_submitting.set()
-    th.join()
+    try:
+        for r in stream:
+            now = time.perf_counter() - t0
+            if r.t_arrival > now:
+                time.sleep(r.t_arrival - now)
+            try:
+                rid = server.submit(r.jet.desc(), r.plane.desc(), r.nu, params)
+            except JetshowError as e:
+                if e.status != A.JSH_ERR_OOM:
+                    raise
+                rejected += 1
+                continue
+            with lock:
+                pending[rid] = r
+    finally:
+        done_submitting.set()
+        th.join()
     wall = time.perf_counter() - t0
+    if counts is not None:
+        counts["submitted"] = len(stream) - rejected
+        counts["admission_rejections"] = rejected
     if errors:
         raise errors[0]
     return records, wall

@@ -12,7 +12,10 @@
   0.1; 1024x1024 at 0.02 mas, 5 and 15.4 GHz.
 
 Every workload returns (Jet, ImagePlane, nu[Hz, source frame], params kw).
-``scale`` shrinks the image (for tests) keeping the physical extent.
+``scale`` shrinks the image (for tests) keeping the physical extent; ``pcm``
+(parsecs per mas at z = 0.1 in the flat cosmology) is computed with the
+library's ``jsh_mas_to_pc`` unless the caller passes it (the CPU reference
+arm of the benchmark passes the oracle's value, which is bitwise the same).
 """
 from __future__ import annotations
 
@@ -31,8 +34,8 @@ def pc_per_mas(z=Z):
     return mas_to_pc(z, **COSMO_FLAT)
 
 
-def _lg_cm(mas, z=Z):
-    return math.log10(mas * pc_per_mas(z) * J.pc)
+def _lg_cm(mas, z=Z, pcm=None):
+    return math.log10(mas * (pcm if pcm is not None else pc_per_mas(z)) * J.pc)
 
 
 def conical_model(half_angle=0.05, b0=0.1, n0=500.0, gamma=10.0, s=2.5, gamma_min=10.0, pitch=math.pi / 4,
@@ -66,36 +69,51 @@ ACCURATE_I_KW = dict(ACCURATE_KW, rtol=1e-7, output="I")
 # 2.2e-4 (tau) / 1.3e-4 (I) off a converged solution at ACCURATE_KW and
 # 1.8e-5 / 1.7e-5 at these settings.
 GRID_KW = dict(ACCURATE_KW, tau_rtol=1e-9, rtol=1e-8)
+# Gridded fields, two implementations of the FP64 algorithm compared with
+# each other: a last-bit difference anywhere (an fma contraction, a libm
+# ulp) moves the adaptive steps across the interpolant's kinks and, at
+# GRID_KW, the two images by up to 2.3e-5 in tau (measured with the oracle
+# against a perturbed copy of itself); at these tolerances by 1e-6.
+GRID_TIGHT_KW = dict(ACCURATE_KW, tau_rtol=1e-11, rtol=1e-10)
+# Gridded fields, mixed precision: the tau pass's steps limited to 0.001 pc
+# (a fifth of a triangle of the 200k-point grid) so that every kink is
+# resolved, and IQUV at rtol 1e-8; measured against the oracle at tau rtol
+# 1e-12 on the simulation-grid jet: tau 7.1e-6, I 5.8e-6, Q/U/V 2.5e-6 of
+# max I (at ACCURATE_KW: 1.3e-4 / 1.6e-4 / 9.9e-5), for 3.1x the work.
+GRID_MIXED_KW = dict(ACCURATE_KW, dt_max=0.001 * J.pc, rtol=1e-8)
 # Converged reference settings (the FP64 oracle at rtol 1e-10).
 CONVERGED_KW = dict(n=100, tau_max=1e4, tau_min=1e-10, tau_atol=1e-20, tau_rtol=1e-10, atol=1e-30, rtol=1e-10,
                     output="full")
+# ... and for gridded fields, whose kinks converge slowly (rtol 1e-10 and
+# 1e-12 differ by 4.9e-6 in tau there)
+GRID_CONVERGED_KW = dict(CONVERGED_KW, tau_rtol=1e-12)
 
 
-def conical_c0(scale=1):
+def conical_c0(scale=1, pcm=None):
     n = max(2, 128 // scale)
     n += n % 2
     mas = 0.1 * 128 / n
-    plane = J.ImagePlane((n, n), _lg_cm(mas), _lg_cm(mas), 0.1)
+    plane = J.ImagePlane((n, n), _lg_cm(mas, pcm=pcm), _lg_cm(mas, pcm=pcm), 0.1)
     nu = np.array([15.4e9]) * (1 + Z)
     return conical_model(), plane, nu, dict(TRANSFER_KW)
 
 
-def conical_c1(scale=1, n_freq=4):
+def conical_c1(scale=1, n_freq=4, pcm=None):
     na, nl = max(2, 512 // scale), max(2, 1024 // scale)
     na += na % 2
-    plane = J.ImagePlane((na, nl), _lg_cm(10 ** -3), _lg_cm(10 ** -1), 0.1)
+    plane = J.ImagePlane((na, nl), _lg_cm(10 ** -3, pcm=pcm), _lg_cm(10 ** -1, pcm=pcm), 0.1)
     nu = np.array([8.1e9, 8.4e9, 12.1e9, 15.4e9][:n_freq]) * (1 + Z)
     return conical_model(), plane, nu, dict(TRANSFER_KW)
 
 
-def parabolic_c2(scale=1, n_freq=2):
+def parabolic_c2(scale=1, n_freq=2, pcm=None):
     n = max(2, 1024 // scale)
     n += n % 2
     mas = 0.02 * 1024 / n
     geo = J.ParabaloidCone((0, 0, 0), (0, 0, 1), 0.1 * J.pc, 1.0 * J.pc, 100.0 * J.pc)
     jet = J.Jet(geo, J.ConstFlatVField(10.0), J.HelicalConicalBField(1.0, 1.0, math.pi / 4, True),
                 J.BKNField(500.0, 2.0, True), s=2.5, gamma_min=10.0, thermal_fraction=0.1)
-    plane = J.ImagePlane((n, n), _lg_cm(mas), _lg_cm(mas), 0.05)
+    plane = J.ImagePlane((n, n), _lg_cm(mas, pcm=pcm), _lg_cm(mas, pcm=pcm), 0.05)
     nu = np.array([5.0e9, 15.4e9][:n_freq]) * (1 + Z)
     return jet, plane, nu, dict(TRANSFER_KW)
 

@@ -752,9 +752,13 @@ double jo_grid_value(int32_t grid_id, int32_t field, double px, double py, doubl
   return nan_value;
 }
 
+/* hypot(x, y) of src/SimulationInterpolater.cpp:49 as sqrt(x*x + y*y), each
+ * operation rounded once (-ffp-contract=off): within an ulp of a libm hypot
+ * at these magnitudes (the reference's libm is unpinned), and the order the
+ * device rounds in, so device and oracle locate the same triangle. */
 static double sim_value(int32_t grid, int32_t field, v3 p, double nan_value) {
   double x = p.x / JO_PC, y = p.y / JO_PC, z = p.z / JO_PC;
-  double r = hypot(x, y);
+  double r = sqrt(x * x + y * y);
   return jo_grid_value(grid, field, z, r, nan_value);
 }
 

@@ -13,10 +13,13 @@ that import line works unchanged and renders on the GB300:
   defaults and return value ([n_across][n_along] numpy arrays instead of
   lists of lists);
 * ``get_iquv_image(...)``: the same model with the full-Stokes pass,
-  returning (tau, I, Q, U, V) in Jy per pixel (new).
+  returning (tau, I, Q, U, V) in Jy per pixel (new);
+* ``get_i_visibilities(..., uv, dx, dy, rot)``: the visibilities of that
+  image at (u, v) points, transformed on the device (JetModelZoom.ft of
+  jetmodel.py:114-132; new).
 
 There is no CPU path: the call needs the built CUDA library and a GB300.
 """
-from jetshow_gb300.pyjetshow import get_i_image, get_iquv_image
+from jetshow_gb300.pyjetshow import get_i_image, get_i_visibilities, get_iquv_image
 
-__all__ = ["get_i_image", "get_iquv_image"]
+__all__ = ["get_i_image", "get_iquv_image", "get_i_visibilities"]

@@ -61,3 +61,12 @@ def test_ctx_create_without_gpu_fails_cleanly(lib):
     else:
         assert st in (A.JSH_ERR_NO_DEVICE, A.JSH_ERR_CUDA)
         assert lib.jsh_last_error()
+
+
+def test_request_h2d_bytes(lib):
+    # the request record plus 8 bytes per frequency, plus the FP32
+    # constants (56 bytes per frequency) for mixed precision
+    b1 = lib.jsh_request_h2d_bytes(1, A.PREC_FP64)
+    assert lib.jsh_request_h2d_bytes(4, A.PREC_FP64) == b1 + 3 * 8
+    assert lib.jsh_request_h2d_bytes(4, A.PREC_MIXED) == b1 + 3 * 8 + 4 * 56
+    assert 1024 < b1 < 4096

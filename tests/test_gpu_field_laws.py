@@ -1,0 +1,112 @@
+"""Every analytic field law of the model, rendered on the GPU against the
+oracle: a small full-Stokes image of the conical jet (two frequencies) with
+one B, N or V law swapped in and the others at the benchmark model's
+(helical conical B, BK n, ConstFlat V).
+
+* FP64 device against the oracle running the same algorithm at tight
+  tolerances (tau rtol 1e-11, IQUV rtol 1e-10): laws with jumps or kinks
+  (sheaths, composite exponents, the atan(y/x) sign flip of ToroidalBField
+  and ForceFree, src/BField.cpp:99-106, :137-146) make the adaptive step
+  sequence sensitive to last-bit differences, and tight tolerances keep the
+  two implementations within the contract gates of each other.
+* Mixed precision (FP32 stages) against the converged oracle (rtol 1e-10)
+  at the accuracy-qualified tolerances.
+Reference quirks reproduced: ShearedCentralVField evaluates acos(z + o_z/r)
+with z in cm (src/VField.cpp:83), a NaN for every point of a real jet: the
+oracle and both device paths flag every hit item JSH_ST_NAN.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from jetshow_gb300 import _capi as A
+from jetshow_gb300 import jet as J
+from jetshow_gb300 import workloads as W
+from helpers import compare_images, flat
+
+pytestmark = pytest.mark.gpu
+
+PC = J.pc
+TIGHT_KW = dict(W.ACCURATE_KW, tau_rtol=1e-11, rtol=1e-10)
+
+B_LAWS = {
+    "RandomScalarBField": lambda: J.RandomScalarBField(0.1, 1.0),
+    "RandomScalarBFieldZ": lambda: J.RandomScalarBFieldZ(0.1, 1.0),
+    "CompositeRandomScalarBFieldZ": lambda: J.CompositeRandomScalarBFieldZ(0.1, 1.0, 1.5, 2.0 * PC),
+    "ConstCylinderBField": lambda: J.ConstCylinderBField(0.1, 1.0, True),
+    "ConstCylinderBFieldZ": lambda: J.ConstCylinderBFieldZ(0.1, 1.0, True),
+    "RadialConicalBField": lambda: J.RadialConicalBField(0.1, 1.0, True),
+    "ToroidalBField": lambda: J.ToroidalBField(0.1, 1.0, True),
+    "ToroidalBField_lab": lambda: J.ToroidalBField(0.1, 1.0, False),
+    "HelicalCylinderBField": lambda: J.HelicalCylinderBField(0.1, math.pi / 4, True),
+    "SpiralConicalBField": lambda: J.SpiralConicalBField(0.01, math.pi / 4, True),
+    "ForceFreeCylindricalBField": lambda: J.ForceFreeCylindricalBField(0.1, 1.0, True),
+    "HelicalConicalBField_atan": lambda: J.HelicalConicalBField(0.1, 1.0, math.pi / 4, True, atan_quirk=True),
+    "HelicalConicalBField_lab": lambda: J.HelicalConicalBField(0.1, 1.0, math.pi / 4, False),
+}
+N_LAWS = {
+    "ConstNField": lambda: J.ConstNField(50.0, True),
+    "BKNField_lab": lambda: J.BKNField(500.0, 2.0, False),
+    "BKNFieldZ": lambda: J.BKNFieldZ(500.0, 2.0, True),
+    "CompositeBKNField": lambda: J.CompositeBKNField(500.0, 2.0, 2.5, 2.0 * PC, True),
+}
+V_LAWS = {
+    "ShearedFlatVField": lambda: J.ShearedFlatVField(10.0, 2.0, 10.0 * PC),
+    "SheathFlatVField": lambda: J.SheathFlatVField(10.0, 3.0, 0.05 * PC),
+    "ConstCentralVField": lambda: J.ConstCentralVField(10.0, (0.0, 0.0, 0.5 * PC)),
+    "ShearedCentralVField": lambda: J.ShearedCentralVField(10.0, 2.0, 0.05),
+    "SheathCentralVField": lambda: J.SheathCentralVField(10.0, 3.0, 0.02),
+    "ConstParabolicVField": lambda: J.ConstParabolicVField(10.0, 0.1 * PC),
+    "AccParabolicVField": lambda: J.AccParabolicVField(10.0, 1.0 * PC, 0.1 * PC),
+    "ShearedAccParabolicVField": lambda: J.ShearedAccParabolicVField(10.0, 2.0, 1.0 * PC, 0.1 * PC),
+    "AccParabolicConstConeVField": lambda: J.AccParabolicConstConeVField(10.0, 0.1 * PC, 1.0 * PC),
+    "ShearedAccParabolicConstConeVField": lambda: J.ShearedAccParabolicConstConeVField(10.0, 2.0, 0.1 * PC,
+                                                                                        1.0 * PC),
+}
+CASES = [("B", k) for k in B_LAWS] + [("N", k) for k in N_LAWS] + [("V", k) for k in V_LAWS]
+
+
+def case_model(kind, name):
+    jet = W.conical_model()
+    if kind == "B":
+        jet.bfield = B_LAWS[name]()
+    elif kind == "N":
+        jet.nfield = N_LAWS[name]()
+    else:
+        jet.vfield = V_LAWS[name]()
+    pcm = W.pc_per_mas()
+    plane = J.ImagePlane((12, 20), math.log10(10 ** -2.5 * pcm * PC), math.log10(10 ** -0.5 * pcm * PC), 0.1)
+    nu = np.array([8.4e9, 15.4e9]) * (1 + W.Z)
+    return jet, plane, nu
+
+
+def check_case(g, r, gate_kw):
+    hit = (r["status"] & A.ST_HIT) != 0
+    assert np.array_equal(hit, (g["status"] & A.ST_HIT) != 0), "hit mask"
+    assert hit.sum() > 50
+    nan_r = (r["status"] & A.ST_NAN) != 0
+    if nan_r[hit].any():
+        # a law whose reference formula is NaN on the jet: flagged alike
+        assert np.array_equal(nan_r, (g["status"] & A.ST_NAN) != 0), "NaN status differs"
+        return None
+    assert not ((g["status"] & A.ST_ERRORS) != 0).any(), hex(int(np.bitwise_or.reduce(g["status"].ravel())))
+    return compare_images(g, r, full=True, tau_max=1e4, **gate_kw)
+
+
+@pytest.mark.parametrize("kind,name", CASES)
+def test_field_law_fp64_vs_oracle(ctx, oracle, kind, name):
+    jet, plane, nu = case_model(kind, name)
+    p = J.make_params(precision="fp64", schedule="static", **TIGHT_KW)
+    g, st = ctx.render(jet.desc(), plane.desc(), nu, p)
+    r = oracle.render(jet.desc(), plane.desc(), nu, p)
+    check_case(flat(g), r, {})
+
+
+@pytest.mark.parametrize("kind,name", CASES)
+def test_field_law_mixed_vs_converged(ctx, oracle, kind, name):
+    jet, plane, nu = case_model(kind, name)
+    g, st = ctx.render(jet.desc(), plane.desc(), nu,
+                       J.make_params(precision="mixed", schedule="persistent", **W.ACCURATE_KW))
+    r = oracle.render(jet.desc(), plane.desc(), nu, J.make_params(**W.CONVERGED_KW))
+    check_case(flat(g), r, {})

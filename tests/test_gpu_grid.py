@@ -24,6 +24,9 @@ def c3(ctx, oracle):
 
 
 def test_interpolation_matches_oracle(ctx, oracle, c3):
+    """Device point location and barycentric value against the oracle's,
+    bit for bit (src/SimulationInterpolater.cpp:43-102), at random points in
+    and outside the grid and at its vertices."""
     gid, xy, vals, tri = c3
     rng = np.random.default_rng(5)
     q = np.column_stack([rng.uniform(-1.0, 21.0, 20000), rng.uniform(-0.05, 0.55, 20000)])
@@ -31,10 +34,9 @@ def test_interpolation_matches_oracle(ctx, oracle, c3):
     for field in range(vals.shape[1]):
         g = ctx.grid_interpolate(gid, field, q, nan_value=NAN)
         r = np.array([oracle.grid_value(gid, field, z, rr, NAN) for z, rr in q])
-        assert np.array_equal(g == NAN, r == NAN), field
-        sel = r != NAN
-        assert sel.sum() > 15000
-        np.testing.assert_allclose(g[sel], r[sel], rtol=1e-12, atol=0)
+        # the same rounding order on both sides: the same triangle, the same bits
+        assert np.array_equal(g, r), field
+        assert (r != NAN).sum() > 15000
         # at a vertex the interpolant is the vertex's FP32 value
         np.testing.assert_allclose(g[-2000:], vals[:2000, field].astype(np.float64), rtol=1e-12)
 
@@ -53,22 +55,32 @@ def test_interpolation_reproduces_linear_field(ctx):
     assert np.all(out == NAN)
 
 
-# The interpolated fields have kinks at every triangle edge, where the
-# adaptive Dormand-Prince steps converge slowly: the FP64 algorithm itself is
-# 1.8e-5 (tau) off a solution at rtol 1e-12 with tau rtol 1e-9 / IQUV rtol
-# 1e-8 (GRID_KW), and 2.2e-4 at the conical jet's qualified tolerances.  The
-# tau gate on this workload is therefore 1e-4 (same algorithm, two
-# implementations) and 5e-4 (mixed at the conical jet's tolerances against a
-# converged solution); the I, Q/U/V and flux gates are the contract's.
+# The interpolated fields have kinks at every triangle edge.  Two
+# implementations of the same FP64 algorithm are compared at GRID_TIGHT_KW
+# (a last-bit difference moves the adaptive steps across the kinks; at these
+# tolerances the two images stay within 1e-6 of each other), on a short jet
+# bounded by the hull of the grid points with 0.5 <= z <= 3 pc (one thread
+# per item on the FP64 pipe: the cost of the heaviest ray sets the test's
+# time).  The mixed path is compared with a converged solution at
+# GRID_MIXED_KW.  Every gate is the contract's.
+
+
+def short_jet(ctx, oracle, c3, scale):
+    gid, xy, _, _ = c3
+    inner = xy[(xy[:, 0] >= 0.5) & (xy[:, 0] <= 3.0) & (xy[:, 1] <= 0.25)]
+    hid = ctx.hull_upload(inner, 36)
+    oracle.hull_register(hid, inner, 36)
+    jet, plane, nu, _ = W.simulation_c3(gid, scale=scale)
+    jet.geometry = J.SimulationGeometry(hid)
+    return jet, plane, nu
 
 
 def test_fp64_simulation_render_vs_oracle(ctx, oracle, c3):
-    gid = c3[0]
-    jet, plane, nu, _ = W.simulation_c3(gid, scale=16)
-    p = J.make_params(precision="fp64", schedule="static", **W.GRID_KW)
+    jet, plane, nu = short_jet(ctx, oracle, c3, 64)
+    p = J.make_params(precision="fp64", schedule="static", **W.GRID_TIGHT_KW)
     g, st = ctx.render(jet.desc(), plane.desc(), nu, p)
     r = oracle.render(jet.desc(), plane.desc(), nu, p)
-    e = compare_images(flat(g), r, full=True, tau_max=1e4, tau_rtol=1e-4)
+    e = compare_images(flat(g), r, full=True, tau_max=1e4)
     assert e["n_hit"] == st["n_hit_pixels"] > 0
     assert np.abs(r["I"]).max() > 0
 
@@ -77,6 +89,6 @@ def test_mixed_simulation_render_vs_converged(ctx, oracle, c3):
     gid = c3[0]
     jet, plane, nu, _ = W.simulation_c3(gid, scale=16)
     g, st = ctx.render(jet.desc(), plane.desc(), nu,
-                       J.make_params(precision="mixed", schedule="persistent", **W.ACCURATE_KW))
-    r = oracle.render(jet.desc(), plane.desc(), nu, J.make_params(**W.CONVERGED_KW))
-    compare_images(flat(g), r, full=True, tau_max=1e4, tau_rtol=5e-4, i_rtol=5e-4)
+                       J.make_params(precision="mixed", schedule="persistent", **W.GRID_MIXED_KW))
+    r = oracle.render(jet.desc(), plane.desc(), nu, J.make_params(**W.GRID_CONVERGED_KW))
+    compare_images(flat(g), r, full=True, tau_max=1e4)

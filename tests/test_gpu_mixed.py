@@ -119,3 +119,28 @@ def test_cost_map_counts_every_evaluation(ctx):
         assert np.all(g["l"][hit] > 0) and np.all(g["l"][~hit] == 0)
         assert np.all(g["l"] == np.round(g["l"]))
         assert int(g["l"].sum()) == st["rhs_evals"]
+
+
+@pytest.mark.parametrize("output", ["full", "I"])
+@pytest.mark.parametrize("flags", [A.FLAG_SINGLE_KERNEL, A.FLAG_TAU_DENSE, A.FLAG_COMPACT_REGS,
+                                   A.FLAG_IQUV_FROM_TAU_MAX])
+def test_split_kernels_match_single_kernel(ctx, flags, output):
+    """The persistent schedule's split form (a tau kernel, then an IQUV kernel
+    over the ranked items that need a second pass) against the static
+    schedule and the single-kernel form: every plane bitwise the same, with
+    each build of the kernels, and with the cost map (the l plane counts
+    the evaluations of both passes)."""
+    jet, plane, nu, _ = W.conical_c1(scale=8)
+    kw = dict(W.ACCURATE_KW, output=output)
+    extra = flags & A.FLAG_IQUV_FROM_TAU_MAX
+    ref, sr = ctx.render(jet.desc(), plane.desc(), nu,
+                         J.make_params(precision="mixed", schedule="static", flags=extra | A.FLAG_COST_MAP, **kw))
+    got, sg = ctx.render(jet.desc(), plane.desc(), nu,
+                         J.make_params(precision="mixed", schedule="persistent", flags=flags | A.FLAG_COST_MAP,
+                                       **kw))
+    for k in ("tau", "l", "I", "Q", "U", "V", "status"):
+        assert np.array_equal(got[k], ref[k]), k
+    assert sg["rhs_evals"] == sr["rhs_evals"] == int(ref["l"].sum())
+    assert (sg["steps_accepted"], sg["steps_rejected"]) == (sr["steps_accepted"], sr["steps_rejected"])
+    if flags != A.FLAG_SINGLE_KERNEL:
+        assert sg["kernels_launched"] == 11

@@ -217,3 +217,26 @@ def test_optically_thin_limit(oracle):
         eta = np.array([oracle.coefficients(m, a + t * (b - a), -d, nu[0])[7] for t in s])
         integral = np.trapezoid(eta, s) * np.linalg.norm(b - a)
         assert abs(r["I"][0][pix] - integral) / integral < 1e-6, (pix, r["I"][0][pix], integral)
+
+
+def test_visibility_direct_sum_known_answers():
+    """The FP64 direct sum of the visibility tests: a single pixel gives
+    F exp(-2 pi i (u' x + v' y)) times the shift; a symmetric pair about the
+    phase centre gives a real visibility 2 F cos(2 pi u' x); the pixel
+    centres follow the image's running-sum / half-integer layout."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from vis_oracle import direct_sum, pixel_centres
+    across, along = pixel_centres([1.0, 2.0, 4.0], 4)
+    assert np.allclose(along[0], [0.5, 2.0, 5.0])
+    assert np.allclose(across[:, 0], [1.5, 0.5, -0.5, -1.5]) and np.allclose(across[:, 2], [6, 2, -2, -6])
+    uv = np.array([[0.0, 0.0], [0.25, 0.0], [0.1, 0.3]])
+    v = direct_sum([2.0], [-3.0], [5.0], uv, 1.0, dx=0.5, dy=0.0, rot=0.0)
+    ph = uv[:, 0] * 3.0 + uv[:, 1] * 5.0 + uv[:, 0] * 0.5
+    assert np.allclose(v, 2.0 * np.exp(-2j * np.pi * ph), atol=1e-14)
+    v2 = direct_sum([1.0, 1.0], [-2.0, 2.0], [0.0, 0.0], uv, 1.0)
+    assert np.allclose(v2.imag, 0, atol=1e-14) and np.allclose(v2.real, 2 * np.cos(2 * np.pi * uv[:, 0] * 2.0))
+    # a rotation by pi/2 maps u' = v, v' = -u
+    v3 = direct_sum([1.0], [-1.0], [0.0], np.array([[0.0, 0.2]]), 1.0, rot=np.pi / 2)
+    assert np.allclose(v3, np.exp(-2j * np.pi * 0.2), atol=1e-14)
