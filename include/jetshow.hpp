@@ -158,6 +158,70 @@ class VectorBField : public Field {
  protected:
   using Field::Field;
 };
+// Random directions added to a vector field: RandomVectorBField and its
+// kinds (src/BField.cpp:149-193).  The wrapper's field is taken in the
+// plasma frame, as the reference's VectorBField(true) base makes it.
+class RandomVectorBField : public VectorBField {
+ public:
+  const jsh_random_desc& random() const { return r_; }
+
+ protected:
+  RandomVectorBField(VectorBField* bfield, double rnd_fraction, int kind) : VectorBField(*bfield) {
+    std::memset(&r_, 0, sizeof(r_));
+    r_.kind = kind;
+    r_.fraction = rnd_fraction;
+  }
+  jsh_random_desc r_;
+};
+
+// RandomCellsInSphere(N, n_exponent, seed) (src/Cells.cpp:24-47): N cells
+// drawn on the host by the counter-based generator (jsh_cells_generate),
+// uploaded by create().
+class RandomCellsInSphere {
+ public:
+  RandomCellsInSphere(int N, double n_exponent, unsigned int seed = 0) : n_(N), exponent_(n_exponent), seed_(seed) {}
+  void setGeometry(double coord1_max, double coord2_max, double coord1_min = 0., double coord2_min = 0.) {
+    r_max_ = coord1_max, theta_max_ = coord2_max, r_min_ = coord1_min, theta_min_ = coord2_min;
+  }
+  void create(jsh_ctx* ctx = default_context()) {
+    points_.assign(3 * (size_t)n_, 0.0);
+    directions_.assign(3 * (size_t)n_, 0.0);
+    check(jsh_cells_generate(n_, r_min_, r_max_, theta_max_, exponent_, seed_, points_.data(), directions_.data()));
+    check(jsh_cells_upload(ctx, points_.data(), directions_.data(), n_, &id_));
+  }
+  const std::vector<double>& getCells() const { return points_; }
+  int32_t id() const { return id_; }
+
+ private:
+  int n_;
+  double exponent_;
+  unsigned int seed_;
+  double r_max_ = 0, theta_max_ = 0, r_min_ = 0, theta_min_ = 0;
+  std::vector<double> points_, directions_;
+  int32_t id_ = -1;
+};
+
+// CellsRandomVectorBField(cells, bfield, rnd_fraction) (src/BField.cpp:164-172).
+class CellsRandomVectorBField : public RandomVectorBField {
+ public:
+  CellsRandomVectorBField(RandomCellsInSphere* cells, VectorBField* bfield, double rnd_fraction)
+      : RandomVectorBField(bfield, rnd_fraction, JSH_RND_CELLS) {
+    if (!cells || cells->id() < 0) throw std::runtime_error("CellsRandomVectorBField: create() the cells first");
+    r_.cells_id = cells->id();
+  }
+};
+
+// PointsRandomVectorBField(bfield, rnd_fraction, seed) (src/BField.cpp:175-193):
+// a fresh direction at every evaluation, keyed by (seed, pixel, frequency,
+// evaluation index) instead of per-thread generators.
+class PointsRandomVectorBField : public RandomVectorBField {
+ public:
+  PointsRandomVectorBField(VectorBField* bfield, double rnd_fraction, unsigned int seed)
+      : RandomVectorBField(bfield, rnd_fraction, JSH_RND_POINTS) {
+    r_.seed = seed;
+  }
+};
+
 class NField : public Field {
  protected:
   using Field::Field;
@@ -338,6 +402,7 @@ class Jet {
     d_.geometry = geo->desc();
     d_.vfield = v->desc();
     d_.bfield = b->desc();
+    if (auto* rb = dynamic_cast<RandomVectorBField*>(b)) d_.random = rb->random();
     d_.nfield = n->desc();
     d_.s = s;
     d_.gamma_min = gmin;

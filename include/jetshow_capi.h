@@ -53,7 +53,7 @@
 extern "C" {
 #endif
 
-#define JSH_ABI_VERSION 1
+#define JSH_ABI_VERSION 2 /* 2: jsh_model_desc.random */
 
 /* ---------------------------------------------------------------- status */
 #define JSH_OK 0
@@ -152,6 +152,31 @@ typedef struct jsh_field_desc {
   double p[8];             /* kind-specific parameters, see the enums */
 } jsh_field_desc;
 
+/* Random directions added to a vector B field: RandomVectorBField::bf
+ * (src/BField.cpp:149-161), B(p) + fraction |B(p)| n(p) with n a unit
+ * vector, the wrapper's B taken as given in the plasma frame (the wrapper
+ * is constructed VectorBField(true)) whatever the wrapped field's flag.
+ *  - JSH_RND_CELLS (CellsRandomVectorBField, src/BField.cpp:164-172): n is
+ *    the direction of the cell nearest to p among the points of a cell set
+ *    uploaded with jsh_cells_upload (RandomCells::getID, src/Cells.cpp:13-18).
+ *  - JSH_RND_POINTS (PointsRandomVectorBField, src/BField.cpp:175-193): a
+ *    fresh direction at every right-hand-side evaluation.  The reference
+ *    draws it from a per-OpenMP-thread Mersenne Twister, so its images
+ *    depend on the thread schedule; here the draw is a counter-based
+ *    function of (seed, pixel, frequency, evaluation index): the same
+ *    render gives the same image, alone or batched with others.
+ * Directions are drawn with Philox4x32-10 (Salmon et al., SC'11) by
+ * rejection from the cube [-1, 1]^3 and normalised in correctly rounded
+ * FP64, so host, device and a C restatement draw the same bits. */
+enum jsh_random_kind { JSH_RND_NONE = 0, JSH_RND_CELLS = 1, JSH_RND_POINTS = 2 };
+
+typedef struct jsh_random_desc {
+  int32_t kind;     /* enum jsh_random_kind */
+  int32_t cells_id; /* JSH_RND_CELLS: id from jsh_cells_upload */
+  double fraction;  /* rnd_fraction of the reference (>= 0) */
+  uint64_t seed;    /* JSH_RND_POINTS: key of the direction stream */
+} jsh_random_desc;
+
 typedef struct jsh_model_desc {
   jsh_geometry_desc geometry;
   jsh_field_desc bfield;
@@ -161,6 +186,7 @@ typedef struct jsh_model_desc {
                               (the reference hard-codes s = 3.42, src/Jet.cpp:32) */
   double gamma_min;        /* low-energy cut-off in k_F_r, k_C_r (src/utils.cpp:86-98) */
   double thermal_fraction; /* n_th / n for cold-plasma k_F_c, k_C_c terms (builder-defined) */
+  jsh_random_desc random;  /* random directions added to a vector B field (kind 0: none) */
 } jsh_model_desc;
 
 /* ----------------------------------------------------------- image plane */
@@ -432,6 +458,34 @@ int jsh_hull_upload(jsh_ctx* ctx, const double* zr, int64_t n, int32_t n_circle,
  * must hold n entries.  Same argument checks as jsh_hull_upload. */
 int jsh_hull_profile(const double* zr, int64_t n, int32_t n_circle, double* vz,
                      double* vR, int32_t* m);
+
+/* ---------------------------------------------------- random cells */
+/* The cells of RandomCellsInSphere::create (src/Cells.cpp:35-47): n points
+ * drawn as generate_random_points_sphere does (src/utils.cpp:267-312):
+ *   r = r_min + (r_max - r_min) U1, phi = 2 pi U2,
+ *   u = (1 - c)(2 U3 - 1) shifted by -c (u < 0) or +c, c = cos(theta_max)
+ *   (c = 1 for theta_max <= 0: every point on the axis, as there),
+ *   theta = acos(u), r = r^(1 / (3 - exponent)),
+ *   point = (r sin theta cos phi, r sin theta sin phi, r cos theta) [cm],
+ * and one random unit direction per cell (generate_random_directions,
+ * src/utils.cpp:249-261).  The reference's Boost Mersenne Twister streams
+ * are replaced by Philox4x32-10 keyed by `seed` (uniforms U = (x + 1/2)
+ * 2^-32 of its 32-bit outputs).  Host only (no context, no device).  All n
+ * points are kept (the reference copies only the first n/2 into its cell
+ * matrix and leaves the rest uninitialised). */
+int jsh_cells_generate(int64_t n, double r_min, double r_max, double theta_max, double exponent, uint64_t seed,
+                       double* points, double* directions);
+/* Upload a cell set (points[n][3] cm, unit directions[n][3]) once; returns
+ * an id for jsh_random_desc.cells_id.  The device finds a point's cell
+ * through a uniform bucket grid whose buckets list every point that can be
+ * nearest inside them (exact: the nearest point, ties to the lowest index). */
+#define JSH_MAX_CELLS 16
+int jsh_cells_upload(jsh_ctx* ctx, const double* points, const double* directions, int64_t n, int32_t* cells_id);
+/* Checks: the nearest cell of each of n host points (cm), found on the
+ * device (out[n]); the random unit directions for n counters keys[n][3]
+ * (k0, k1, k2) of `seed`, drawn on the device (out[n][3]). */
+int jsh_cells_nearest(jsh_ctx* ctx, int32_t cells_id, const double* points, int64_t n, int32_t* out);
+int jsh_random_directions(jsh_ctx* ctx, uint64_t seed, const uint32_t* keys, int64_t n, double* out);
 
 /* --------------------------------------------------------- serving */
 typedef struct jsh_server jsh_server;

@@ -99,6 +99,18 @@ class FieldDesc(C.Structure):
     ]
 
 
+RND_NONE, RND_CELLS, RND_POINTS = 0, 1, 2
+
+
+class RandomDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("cells_id", C.c_int32),
+        ("fraction", C.c_double),
+        ("seed", C.c_uint64),
+    ]
+
+
 class ModelDesc(C.Structure):
     _fields_ = [
         ("geometry", GeometryDesc),
@@ -108,6 +120,7 @@ class ModelDesc(C.Structure):
         ("s", C.c_double),
         ("gamma_min", C.c_double),
         ("thermal_fraction", C.c_double),
+        ("random", RandomDesc),
     ]
 
 
@@ -269,6 +282,11 @@ SIGNATURES = [
      [C.c_void_p, C.c_int32, C.c_int32, _D, C.c_int64, C.c_double, _D]),
     ("jsh_hull_upload", C.c_int, [C.c_void_p, _D, C.c_int64, C.c_int32, _P(C.c_int32)]),
     ("jsh_hull_profile", C.c_int, [_D, C.c_int64, C.c_int32, _D, _D, _P(C.c_int32)]),
+    ("jsh_cells_generate", C.c_int,
+     [C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint64, _D, _D]),
+    ("jsh_cells_upload", C.c_int, [C.c_void_p, _D, _D, C.c_int64, _P(C.c_int32)]),
+    ("jsh_cells_nearest", C.c_int, [C.c_void_p, C.c_int32, _D, C.c_int64, _P(C.c_int32)]),
+    ("jsh_random_directions", C.c_int, [C.c_void_p, C.c_uint64, _P(C.c_uint32), C.c_int64, _D]),
     ("jsh_server_create", C.c_int, [C.c_void_p, _P(ServerConfig), _P(C.c_void_p)]),
     ("jsh_server_destroy", None, [C.c_void_p]),
     ("jsh_server_submit", C.c_int,

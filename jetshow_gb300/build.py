@@ -21,7 +21,7 @@ REPO = os.path.dirname(HERE)
 LIB = os.path.join(OUT, "libjetshow_gb300.so")
 
 CU_SOURCES = ["jsh_kernels.cu", "jsh_fp64.cu", "jsh_persistent.cu", "jsh_noalloc.cu", "jsh_stripe.cu", "jsh_visibility.cu"]
-CPP_SOURCES = ["jsh_host.cpp", "jsh_capi.cpp", "jsh_server.cpp", "jsh_autotune.cpp", "jsh_grid.cpp", "jsh_hull.cpp"]
+CPP_SOURCES = ["jsh_host.cpp", "jsh_capi.cpp", "jsh_server.cpp", "jsh_autotune.cpp", "jsh_grid.cpp", "jsh_hull.cpp", "jsh_cells.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

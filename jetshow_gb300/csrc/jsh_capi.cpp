@@ -192,6 +192,8 @@ int jsh_prepare_request(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_pla
   }
   st = jsh_resolve_hull(ctx, &req->model);
   if (st) return st;
+  st = jsh_resolve_cells(ctx, &req->model);
+  if (st) return st;
   // gridded fields
   int gids[3] = {req->model.grid_b, req->model.grid_n, req->model.grid_v};
   for (int k = 0; k < 3; ++k) {
@@ -284,6 +286,8 @@ extern "C" void jsh_ctx_destroy(jsh_ctx* c) {
   for (auto& g : c->grids)
     if (g.used) jsh_free_device(c, g.mem, g.bytes);
   for (auto& h : c->hulls)
+    if (h.used) jsh_free_device(c, h.mem, h.bytes);
+  for (auto& h : c->cells)
     if (h.used) jsh_free_device(c, h.mem, h.bytes);
   if (c->h_req) cudaFreeHost(c->h_req);
   if (c->h_fc) cudaFreeHost(c->h_fc);

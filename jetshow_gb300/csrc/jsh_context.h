@@ -29,6 +29,13 @@ struct JshGridSlot {
   size_t bytes = 0;
 };
 
+struct JshCellSlot {
+  std::atomic<bool> used{false};
+  JshCells view{};
+  void* mem = nullptr;  // one allocation holding every array of the cell set
+  size_t bytes = 0;
+};
+
 struct JshHullSlot {
   std::atomic<bool> used{false};
   JshHull view{};
@@ -60,6 +67,7 @@ struct jsh_ctx {
   unsigned long long* h_counters = nullptr;  // pinned [8]
   JshGridSlot grids[JSH_MAX_GRIDS];
   JshHullSlot hulls[JSH_MAX_HULLS];
+  JshCellSlot cells[JSH_MAX_CELL_SETS];
   bool tuned = false;
   JshLaunchShape shape{128, 0, 8, 0};
   jsh_stats last{};
@@ -99,6 +107,10 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
 // the compiled model (JSH_ERR_NOT_FOUND for an unknown id); no-op for the
 // analytic geometries.  Called with ctx->mu held.
 int jsh_resolve_hull(jsh_ctx* ctx, JshModel* model);
+// Random cell set: copy the context's view of model->cells_id into the
+// compiled model (JSH_ERR_NOT_FOUND for an unknown id, JSH_ERR_INVALID
+// without a context); no-op for other models.
+int jsh_resolve_cells(jsh_ctx* ctx, JshModel* model);
 // Counters of the last enqueued request (synchronises with it).
 int collect_stats(jsh_ctx* ctx, jsh_stats* s);
 void jsh_set_error(const char* fmt, ...);

@@ -8,6 +8,7 @@
 #pragma once
 
 #include "jsh_geometry.cuh"
+#include "jsh_random.h"
 
 namespace jsh {
 
@@ -240,6 +241,56 @@ __device__ inline double nfield(const JshModel& m, D3 p) {
   }
 }
 
+// ------------------------------------------------------- random directions
+// The cell nearest to p [cm] (RandomCells::getID, src/Cells.cpp:13-18: the
+// smallest squared distance, the lowest index among equals), the squared
+// distances rounded in a fixed order; p's bucket lists every cell that can
+// be nearest inside it, a point outside the grid scans every cell.
+__device__ inline int cells_nearest64(const JshCells& C, D3 p) {
+  const double fx = __ddiv_rn(__dsub_rn(p.x, C.x0), C.h), fy = __ddiv_rn(__dsub_rn(p.y, C.y0), C.h),
+               fz = __ddiv_rn(__dsub_rn(p.z, C.z0), C.h);
+  const bool inside = fx >= 0.0 && fy >= 0.0 && fz >= 0.0 && fx < (double)C.nbx && fy < (double)C.nby &&
+                      fz < (double)C.nbz;
+  int q0 = 0, q1 = C.n;
+  const int32_t* list = nullptr;
+  if (inside) {
+    const int b = ((int)fz * C.nby + (int)fy) * C.nbx + (int)fx;
+    q0 = C.bstart[b];
+    q1 = C.bstart[b + 1];
+    list = C.bitems;
+  }
+  double best = INFINITY;
+  int bi = 0;
+  for (int q = q0; q < q1; ++q) {
+    const int c = list ? list[q] : q;
+    const double dx = __dsub_rn(p.x, C.p[3 * c]), dy = __dsub_rn(p.y, C.p[3 * c + 1]),
+                 dz = __dsub_rn(p.z, C.p[3 * c + 2]);
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (d2 < best) {
+      best = d2;
+      bi = c;
+    }
+  }
+  return bi;
+}
+
+// RandomVectorBField::bf (src/BField.cpp:154-161): b + fraction |b| n, n the
+// nearest cell's direction or a fresh counter-based draw keyed by (pixel,
+// frequency, evaluation index).
+__device__ inline D3 brandom64(const JshModel& m, D3 b, D3 p, uint32_t k0, uint32_t k1, uint32_t k2) {
+  double n[3];
+  if (m.rnd_kind == JSH_RND_CELLS) {
+    const int c = cells_nearest64(m.cells, p);
+    n[0] = m.cells.dir[3 * c];
+    n[1] = m.cells.dir[3 * c + 1];
+    n[2] = m.cells.dir[3 * c + 2];
+  } else {
+    jsh_random_direction(m.rnd_seed, k0, k1, k2, n);
+  }
+  const double f = m.rnd_frac * norm(b);
+  return d3(b.x + f * n[0], b.y + f * n[1], b.z + f * n[2]);
+}
+
 // ------------------------------------------------------- coefficients
 enum { CK_I = 0, CK_Q, CK_V, CK_F, CK_C, CE_I, CE_Q, CE_V, NCOEF };
 
@@ -247,8 +298,11 @@ enum { CK_I = 0, CK_Q, CK_V, CK_F, CK_C, CE_I, CE_Q, CE_V, NCOEF };
 // k = k'/D and eta = eta' D D with k', eta' evaluated on the plasma-frame
 // B', n', nu' = nu/D and n_los'.  kU = etaU = hQ = 0 (src/utils.cpp:67-69,
 // :101-103, :136-138) and are not stored.  FULL = false computes kI, etaI.
+// (rk0, rk1, rk2): key of a per-evaluation random direction (pixel,
+// frequency, evaluation index), used by JSH_RND_POINTS only.
 template <bool FULL>
-__device__ inline void coefficients64(const JshModel& m, D3 p, D3 nl, double nu, double* k) {
+__device__ inline void coefficients64(const JshModel& m, D3 p, D3 nl, double nu, double* k, uint32_t rk0 = 0,
+                                      uint32_t rk1 = 0, uint32_t rk2 = 0) {
   D3 v = vfield(m, p);
   D3 beta = v / JSH_C;
   double gamma = sqrt(1. / (1. - dot(beta, beta)));
@@ -274,6 +328,7 @@ __device__ inline void coefficients64(const JshModel& m, D3 p, D3 nl, double nu,
     return;
   }
   D3 bl = bvector(m, p);
+  if (m.rnd_kind != JSH_RND_NONE) bl = brandom64(m, bl, p, rk0, rk1, rk2);
   D3 b;
   if (m.b_plasma) {
     b = bl;

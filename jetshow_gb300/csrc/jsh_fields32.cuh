@@ -19,6 +19,7 @@
 // 1 - beta = 1 / (Gamma^2 (1 + beta)) stays accurate in FP32.
 #pragma once
 
+#include "jsh_random.h"
 #include "jsh_request.h"
 
 namespace jsh {
@@ -274,6 +275,53 @@ __device__ inline F3 bvector32(const JshModel& m, const JshMixed& X, F3 p) {
   }
 }
 
+// ------------------------------------------------------- random directions
+// The cell nearest to p [pc] in FP32 (the lowest index among equal
+// distances): the mixed path's own position is FP32, so a point within its
+// rounding of a face between two cells may take either neighbour.
+__device__ inline int cells_nearest32(const JshCells& C, F3 p) {
+  const float fx = (p.x - C.x0f) * C.inv_hf, fy = (p.y - C.y0f) * C.inv_hf, fz = (p.z - C.z0f) * C.inv_hf;
+  const bool inside = fx >= 0.f && fy >= 0.f && fz >= 0.f && fx < (float)C.nbx && fy < (float)C.nby &&
+                      fz < (float)C.nbz;
+  int q0 = 0, q1 = C.n;
+  const int32_t* list = nullptr;
+  if (inside) {
+    const int b = (min((int)fz, C.nbz - 1) * C.nby + min((int)fy, C.nby - 1)) * C.nbx + min((int)fx, C.nbx - 1);
+    q0 = C.bstart[b];
+    q1 = C.bstart[b + 1];
+    list = C.bitems;
+  }
+  float best = INFINITY;
+  int bi = 0;
+  for (int q = q0; q < q1; ++q) {
+    const int c = list ? list[q] : q;
+    const F3 d = p - f3(C.pf[3 * c], C.pf[3 * c + 1], C.pf[3 * c + 2]);
+    const float d2 = fdot(d, d);
+    if (d2 < best) {
+      best = d2;
+      bi = c;
+    }
+  }
+  return bi;
+}
+
+// RandomVectorBField::bf (src/BField.cpp:154-161) in FP32: B + fraction |B| n
+// with the nearest cell's direction or the per-evaluation draw of the key
+// (pixel of hit h, frequency f, evaluation index e).
+__device__ inline F3 brandom32(const JshRequest& R, F3 B, F3 p, uint32_t h, uint32_t f, uint32_t e) {
+  const JshModel& m = R.model;
+  F3 n;
+  if (m.rnd_kind == JSH_RND_CELLS) {
+    const int c = cells_nearest32(m.cells, p);
+    n = f3(m.cells.dirf[3 * c], m.cells.dirf[3 * c + 1], m.cells.dirf[3 * c + 2]);
+  } else {
+    double nd[3];
+    jsh_random_direction(m.rnd_seed, (uint32_t)R.hits[h].pix, f, e, nd);
+    n = f3((float)nd[0], (float)nd[1], (float)nd[2]);
+  }
+  return B + n * ((float)m.rnd_frac * sqrtf(fdot(B, B)));
+}
+
 // ------------------------------------------------------- coefficients
 struct Coef32 {
   float kI, kQ, kV, kF, kC, eI, eQ, eV;
@@ -367,7 +415,10 @@ __device__ __forceinline__ void coef32_helical_log(const JshMixed& X, const JshF
   c.kC = fmaf(F.r_kc, c.kI, -F.ac * F.c1 * n_ * (w * w));
 }
 
-__device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqConst& F, F3 p, int mode, Coef32& c) {
+// (rk_h, rk_f, rk_e): hit index, frequency and evaluation index of the
+// per-evaluation random direction (JSH_RND_POINTS only).
+__device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqConst& F, F3 p, int mode, Coef32& c,
+                                          uint32_t rk_h = 0, uint32_t rk_f = 0, uint32_t rk_e = 0) {
   const JshModel& m = R.model;
   const JshMixed& X = R.mix;
   if (X.helical_log) {
@@ -442,6 +493,7 @@ __device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqCons
     }
     B = bvector32(m, X, p);
   }
+  if (m.rnd_kind != JSH_RND_NONE) B = brandom32(R, B, p, rk_h, rk_f, rk_e);
   if (!m.b_plasma) {
     // B' = B / Gamma + Gamma beta^2 / (1 + Gamma) v_hat (v_hat . B)
     B = B * (1.f / gamma) + vdir * (gamma * beta * beta / (1.f + gamma) * fdot(vdir, B));

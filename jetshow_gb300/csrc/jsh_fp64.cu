@@ -31,8 +31,8 @@ __global__ void __launch_bounds__(128) transfer_static64_kernel(const JshRequest
     int f = (int)(local / nhit);
     unsigned h = (unsigned)(local % nhit);
     const JshHit& H = R.hits[h];
-    if (R.P.full) transfer_item64<true>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
-    else transfer_item64<false>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
+    if (R.P.full) transfer_item64<true>(R.model, R.plane, R.P, H, R.nu[f], f, o, tot);
+    else transfer_item64<false>(R.model, R.plane, R.P, H, R.nu[f], f, o, tot);
     if (R.P.flags & JSH_FLAG_COST_MAP) o.l = (double)tot.evals;
     write_item(R, f, H.pix, o);
   }
@@ -56,8 +56,8 @@ __global__ void __launch_bounds__(128) transfer_queue64_kernel(const JshRequest*
     const JshHit& H = R.hits[(unsigned)(local % nhit)];
     Ctl64 tot{0, 0, 0, 0, 0, 0, 0};
     ItemOut o;
-    if (R.P.full) transfer_item64<true>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
-    else transfer_item64<false>(R.model, R.plane, R.P, H, R.nu[f], o, tot);
+    if (R.P.full) transfer_item64<true>(R.model, R.plane, R.P, H, R.nu[f], f, o, tot);
+    else transfer_item64<false>(R.model, R.plane, R.P, H, R.nu[f], f, o, tot);
     uint64_t q = (uint64_t)f * R.npix + (uint64_t)H.pix;
     if (R.tau) R.tau[q] = o.tau;
     if (R.l) R.l[q] = (R.P.flags & JSH_FLAG_COST_MAP) ? (double)tot.evals : o.l;

@@ -254,6 +254,30 @@ int jsh_compile_model(const jsh_model_desc* d, JshModel* m) {
     m->le_v = log2(JSH_PI * cp * m->fe_v * JSH_M_E / JSH_C) + (1. + s / 2.) * log2(cb);
     m->lk_cr_b = ((s - 2.) / 2.) * log2(cb);
   }
+  // random directions (RandomVectorBField): vector fields only; the wrapper
+  // is a plasma-frame field whatever the wrapped one's flag
+  // (src/BField.cpp:149-152)
+  const jsh_random_desc& rd = d->random;
+  m->rnd_kind = rd.kind;
+  m->cells_id = -1;
+  if (rd.kind != JSH_RND_NONE) {
+    if (rd.kind != JSH_RND_CELLS && rd.kind != JSH_RND_POINTS) {
+      jsh_set_error("unknown random-field kind %d", rd.kind);
+      return JSH_ERR_INVALID;
+    }
+    if (m->b_scalar) {
+      jsh_set_error("random directions wrap a vector B field (RandomVectorBField takes a VectorBField)");
+      return JSH_ERR_INVALID;
+    }
+    if (!std::isfinite(rd.fraction) || !(rd.fraction >= 0.0)) {
+      jsh_set_error("random fraction must be finite and >= 0");
+      return JSH_ERR_INVALID;
+    }
+    m->rnd_frac = rd.fraction;
+    m->rnd_seed = rd.seed;
+    m->b_plasma = 1;
+    if (rd.kind == JSH_RND_CELLS) m->cells_id = rd.cells_id;
+  }
   m->full_capable = 1;
   return JSH_OK;
 }

@@ -191,6 +191,19 @@ __global__ void peak_fp64_kernel(double* out, int iters, double a) {
   if (s == 12345.0) out[0] = s;
 }
 
+// ------------------------------------------------------- random cells
+__global__ void cells_nearest_kernel(JshCells C, const double* __restrict__ pts, int64_t n, int32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = cells_nearest64(C, d3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
+}
+
+__global__ void random_dir_kernel(uint64_t seed, const uint32_t* __restrict__ keys, int64_t n, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  jsh_random_direction(seed, keys[3 * i], keys[3 * i + 1], keys[3 * i + 2], out + 3 * i);
+}
+
 }  // namespace
 
 cudaError_t jsh_run_peaks(int num_sms, double* fp32_tflops, double* mufu_tops, double* fp64_tflops,
@@ -288,5 +301,19 @@ cudaError_t jsh_launch_grid_interp(const JshGrid& grid, int field, const double*
                                    double* d_out, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   grid_interp_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(grid, field, d_zr, n, nan_value, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t jsh_launch_cells_nearest(const JshCells& cells, const double* d_pts, int64_t n, int32_t* d_out,
+                                     cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  cells_nearest_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(cells, d_pts, n, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t jsh_launch_random_directions(uint64_t seed, const uint32_t* d_keys, int64_t n, double* d_out,
+                                         cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  random_dir_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(seed, d_keys, n, d_out);
   return cudaGetLastError();
 }

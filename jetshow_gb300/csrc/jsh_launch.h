@@ -54,3 +54,10 @@ cudaError_t jsh_launch_grid_interp(const JshGrid& grid, int field, const double*
 // single-kernel form; compact: its register-capped build; 0 if it cannot run
 // block_size threads).
 int jsh_persistent_occupancy(int precision, bool full, int block_size, bool compact = false, bool single = false);
+
+// Nearest cell of n points (cm) of an uploaded cell set (checks), and the
+// random unit directions of n counters (k0, k1, k2) of `seed`.
+cudaError_t jsh_launch_cells_nearest(const JshCells& cells, const double* d_pts, int64_t n, int32_t* d_out,
+                                     cudaStream_t stream);
+cudaError_t jsh_launch_random_directions(uint64_t seed, const uint32_t* d_keys, int64_t n, double* d_out,
+                                         cudaStream_t stream);

@@ -19,6 +19,7 @@
 #define JSH_MAS_TO_RAD 4.84813681109536e-09
 
 #define JSH_MAX_GRIDS 16
+#define JSH_MAX_CELL_SETS 16
 #define JSH_MAX_SEG 2
 
 struct JshCone {
@@ -57,6 +58,23 @@ struct JshHull {
   double z_min, z_max;
 };
 
+// Device view of an uploaded random cell set (CellsRandomVectorBField): the
+// cell points (cm, FP64, and pc in FP32 for the mixed path), their unit
+// directions, and a uniform bucket grid over the points' box grown by a
+// quarter of its size on every side whose buckets list every point that can
+// be the nearest one inside them; a query outside the grid scans every cell.
+struct JshCells {
+  const double* p;        // [n][3] cm
+  const float* pf;        // [n][3] pc
+  const double* dir;      // [n][3]
+  const float* dirf;      // [n][3]
+  const int32_t* bstart;  // [nbx*nby*nbz + 1]
+  const int32_t* bitems;  // cell ids, ascending within a bucket
+  int32_t n, nbx, nby, nbz;
+  double x0, y0, z0, h;   // grid origin and bucket side [cm]
+  float x0f, y0f, z0f, inv_hf;  // the same in pc (FP32)
+};
+
 struct JshModel {
   // geometry
   int32_t geo_kind;
@@ -84,6 +102,11 @@ struct JshModel {
   int32_t grid_b, grid_n, grid_v;
   int32_t fb_p, fb_phi, f_n, f_v;
   JshGrid grids[3];       // [0]=B grid, [1]=N grid, [2]=V grid (copies of the views)
+  // random directions added to a vector B (RandomVectorBField)
+  int32_t rnd_kind, cells_id;
+  double rnd_frac;
+  uint64_t rnd_seed;
+  JshCells cells;         // JSH_RND_CELLS (copy of the context's view)
 };
 
 struct JshPlane {

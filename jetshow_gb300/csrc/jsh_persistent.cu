@@ -278,6 +278,7 @@ __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict
   L.x[0] = L.x[1] = L.x[2] = L.x[3] = 0.f;
   L.status = (uint32_t)H.status | JSH_ST_HIT;
   L.evals = L.acc = L.rej = 0;
+  L.evals0 = 0;
   begin_tau_segment(L, R, H);
 }
 
@@ -415,9 +416,10 @@ __device__ __noinline__ double crossing_time(double tau_old, double t_old, doubl
 // magnitude of the terms summed into the derivatives (eta_I + k_I |I| for
 // the Stokes vector, k_I for tau): the scale of their FP32 rounding noise.
 __device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& F, bool tau, bool full, bool kionly,
-                                       F3 p, const float* y, float cs, float sn, float* dk, float& kI) {
+                                       F3 p, const float* y, float cs, float sn, float* dk, float& kI, uint32_t rk_h,
+                                       uint32_t rk_f, uint32_t rk_e) {
   Coef32 c;
-  coef32_rt(R, F, p, kionly ? COEF_KI : (full ? COEF_FULL : COEF_I), c);
+  coef32_rt(R, F, p, kionly ? COEF_KI : (full ? COEF_FULL : COEF_I), c, rk_h, rk_f, rk_e);
   kI = c.kI;
   if (tau) {
     dk[0] = c.kI;
@@ -596,7 +598,8 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     const float h = L.dt;
     float dk[5];
     if (!L.init) {
-      L.s1 = rhs32(R, F, tau, coef_full, tau && warp_tau, pn, L.x, c0, s0, dk, L.kI1);
+      L.s1 = rhs32(R, F, tau, coef_full, tau && warp_tau, pn, L.x, c0, s0, dk, L.kI1, L.h, (uint32_t)L.f,
+                   L.evals0 + L.evals);
 #pragma unroll
       for (int c = 0; c < NK; ++c) L.k1[c] = dk[c];
       L.evals++;
@@ -620,7 +623,8 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
         cs = c0 * cd - s0 * sd;
         sn = s0 * cd + c0 * sd;
       }
-      const float sc = rhs32(R, F, tau, coef_full, tau && warp_tau, pn + dirf * (c_C[s] * h), y, cs, sn, dk, kI7);
+      const float sc = rhs32(R, F, tau, coef_full, tau && warp_tau, pn + dirf * (c_C[s] * h), y, cs, sn, dk, kI7,
+                             L.h, (uint32_t)L.f, L.evals0 + L.evals + (uint32_t)(s - 1));
       smax = fmaxf(smax, sc);
       s7 = sc;
 #pragma unroll
@@ -1312,7 +1316,7 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
     double D = 1. / (gamma * (1. - beta * nz));
     double f = (D + 1.) * (gamma / (gamma + 1.));
     X.v_const = 1;
-    X.helical_bk = (m.b_kind == JSH_B_HELICAL_CONICAL && m.n_kind == JSH_N_BK) ? 1 : 0;
+    X.helical_bk = (m.b_kind == JSH_B_HELICAL_CONICAL && m.n_kind == JSH_N_BK && m.rnd_kind == JSH_RND_NONE) ? 1 : 0;
     const double n0p = m.n_plasma ? m.np[0] : m.np[0] / gamma;
     X.helical_log = (X.helical_bk && m.b_plasma && m.bp[0] != 0.0 && n0p > 0.0) ? 1 : 0;
     if (X.helical_log) {

@@ -95,6 +95,8 @@ __device__ __forceinline__ double dt_increase(double dt, double err, double max_
 struct Path64 {
   D3 p0, dir, nl;
   double nu;
+  uint32_t rk0, rk1;  // random-direction key of the item: pixel, frequency
+  uint32_t* ev;       // the item's evaluation counter (NULL: key index 0)
 };
 
 template <int DIM, bool FULL>
@@ -104,12 +106,13 @@ struct Rhs64 {
                                               const double* x, double* dx) {
     D3 p = P.p0 + P.dir * t;
     double k[NCOEF];
+    const uint32_t ev = P.ev ? (*P.ev)++ : 0u;
     if (tau) {
-      coefficients64<false>(m, p, P.nl, P.nu, k);
+      coefficients64<false>(m, p, P.nl, P.nu, k, P.rk0, P.rk1, ev);
       dx[0] = k[CK_I];
       return;
     }
-    coefficients64<FULL>(m, p, P.nl, P.nu, k);
+    coefficients64<FULL>(m, p, P.nl, P.nu, k, P.rk0, P.rk1, ev);
     if (!FULL) {
       dx[0] = k[CE_I] - k[CK_I] * x[0];
       return;
@@ -214,7 +217,8 @@ struct ItemOut {
 // The transfer of one hit ray at one frequency.
 template <bool FULL>
 __device__ void transfer_item64(const JshModel& m, const JshPlane& pl, const JshParamsDev& Pp, const JshHit& hit,
-                                double nu, ItemOut& o, Ctl64& tot) {
+                                double nu, int f, ItemOut& o, Ctl64& tot) {
+  uint32_t ev = 0;  // evaluation index of the item (random-direction key)
   o.tau = o.l = 0.0;
   o.iquv[0] = o.iquv[1] = o.iquv[2] = o.iquv[3] = 0.0;
   o.status = (uint32_t)hit.status | JSH_ST_HIT;
@@ -237,7 +241,7 @@ __device__ void transfer_item64(const JshModel& m, const JshPlane& pl, const Jsh
     D3 dd = pout - pin;
     double length = sqrt((dd.x * dd.x + dd.y * dd.y) + dd.z * dd.z);
     double dt = length / Pp.n;
-    Path64 P{pin, rd, nl, nu};
+    Path64 P{pin, rd, nl, nu, (uint32_t)hit.pix, (uint32_t)f, &ev};
     Ctl64 C{Pp.tau_atol, Pp.tau_rtol, Pp.dt_max, max_steps, 0, 0, 0};
     double t = 0.0, x[1] = {0.0}, k[7][1], x_old[1] = {0.0}, k1_old[1] = {0.0}, dt_used = 0.0, t_old = 0.0;
     bool init = false, crossed = false;
@@ -316,7 +320,7 @@ __device__ void transfer_item64(const JshModel& m, const JshPlane& pl, const Jsh
     double auto_n = Pp.n;
     if (background_tau > 0.1) auto_n = steps_schedule(background_tau, Pp.n, 10 * Pp.n);
     double dt = length / auto_n;
-    Path64 P{pout, nl, nl, nu};
+    Path64 P{pout, nl, nl, nu, (uint32_t)hit.pix, (uint32_t)f, &ev};
     Ctl64 C{Pp.atol, Pp.rtol, 0.0, max_steps, 0, 0, 0};
     double t = 0.0, k[7][DIM], x_old[DIM], k1_old[DIM], dt_used;
     int64_t nsteps = 0;

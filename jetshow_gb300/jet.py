@@ -212,6 +212,90 @@ class SimulationBField(_Field):
         super().__init__(grid_id, field_p, field_phi, in_plasma_frame=in_plasma_frame)
 
 
+class RandomVectorBField:
+    """RandomVectorBField(bfield, rnd_fraction) -- src/BField.cpp:149-161:
+    B + rnd_fraction |B| n with n a random unit vector; the wrapper's field
+    is taken in the plasma frame (the reference constructs it
+    VectorBField(true)).  Use one of the two kinds below."""
+    kind_random = A.RND_NONE
+
+    def __init__(self, bfield, rnd_fraction):
+        if getattr(bfield, "kind", None) in A.SCALAR_B_KINDS:
+            raise ValueError("RandomVectorBField wraps a vector B field")
+        self.bfield, self.rnd_fraction = bfield, float(rnd_fraction)
+
+    def desc(self) -> A.FieldDesc:
+        return self.bfield.desc()
+
+    def random_desc(self) -> A.RandomDesc:
+        return A.RandomDesc(kind=self.kind_random, fraction=self.rnd_fraction)
+
+
+class CellsRandomVectorBField(RandomVectorBField):
+    """CellsRandomVectorBField(cells, bfield, rnd_fraction) --
+    src/BField.cpp:164-172: n is the direction of the cell nearest to the
+    point.  ``cells``: an uploaded RandomCells (or its cell-set id)."""
+    kind_random = A.RND_CELLS
+
+    def __init__(self, cells, bfield, rnd_fraction):
+        super().__init__(bfield, rnd_fraction)
+        self.cells = cells
+
+    def random_desc(self) -> A.RandomDesc:
+        cid = self.cells if isinstance(self.cells, int) else self.cells.id
+        if cid is None:
+            raise RuntimeError("upload the cells first (RandomCells.upload)")
+        return A.RandomDesc(kind=self.kind_random, cells_id=int(cid), fraction=self.rnd_fraction)
+
+
+class PointsRandomVectorBField(RandomVectorBField):
+    """PointsRandomVectorBField(bfield, rnd_fraction, seed) --
+    src/BField.cpp:175-193: a fresh random direction at every evaluation,
+    drawn here from a counter-based stream keyed by (seed, pixel, frequency,
+    evaluation index) instead of the reference's per-thread generators."""
+    kind_random = A.RND_POINTS
+
+    def __init__(self, bfield, rnd_fraction, seed=0):
+        super().__init__(bfield, rnd_fraction)
+        self.seed = int(seed)
+
+    def random_desc(self) -> A.RandomDesc:
+        return A.RandomDesc(kind=self.kind_random, fraction=self.rnd_fraction, seed=self.seed)
+
+
+class RandomCellsInSphere:
+    """RandomCellsInSphere(N, n_exponent, seed) -- src/Cells.cpp:24-47:
+    ``setGeometry(r_max, theta_max, r_min, theta_min)`` then ``create()``
+    draws N cell points (generate_random_points_sphere, src/utils.cpp:267-312)
+    and directions with the counter-based generator on the host
+    (jsh_cells_generate); ``upload(ctx)`` puts them on the device."""
+
+    def __init__(self, N, n_exponent, seed=0):
+        self.n, self.exponent, self.seed = int(N), float(n_exponent), int(seed)
+        self.r_max = self.theta_max = self.r_min = self.theta_min = 0.0
+        self.points = self.directions = None
+        self.id = None
+
+    def setGeometry(self, coord1_max, coord2_max, coord1_min=0.0, coord2_min=0.0):
+        self.r_max, self.theta_max, self.r_min, self.theta_min = (float(coord1_max), float(coord2_max),
+                                                                  float(coord1_min), float(coord2_min))
+
+    def create(self):
+        from .runtime import cells_generate
+        self.points, self.directions = cells_generate(self.n, self.r_min, self.r_max, self.theta_max,
+                                                      self.exponent, self.seed)
+        return self
+
+    def getCells(self):
+        return self.points
+
+    def upload(self, ctx=None):
+        if self.points is None:
+            self.create()
+        self.id = (ctx or default_context()).cells_upload(self.points, self.directions)
+        return self.id
+
+
 class ConstNField(_Field):
     kind = A.N_CONST
 
@@ -348,9 +432,10 @@ class Jet:
         self.s, self.gamma_min, self.thermal_fraction = float(s), float(gamma_min), float(thermal_fraction)
 
     def desc(self) -> A.ModelDesc:
+        rnd = self.bfield.random_desc() if hasattr(self.bfield, "random_desc") else A.RandomDesc()
         return A.ModelDesc(geometry=self.geometry.desc(), bfield=self.bfield.desc(),
                            nfield=self.nfield.desc(), vfield=self.vfield.desc(), s=self.s,
-                           gamma_min=self.gamma_min, thermal_fraction=self.thermal_fraction)
+                           gamma_min=self.gamma_min, thermal_fraction=self.thermal_fraction, random=rnd)
 
     def hit(self, origins, directions, ctx=None):
         """Jet::hit for arrays of rays; returns (n_seg, seg[n, 2, 2, 3], status)."""

@@ -171,6 +171,32 @@ class Context:
                                                  C.byref(hid)))
         return hid.value
 
+    def cells_upload(self, points, directions) -> int:
+        """Upload a random cell set (points [n, 3] cm, unit directions [n, 3])
+        for CellsRandomVectorBField; returns its id."""
+        p = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        d = np.ascontiguousarray(directions, dtype=np.float64).reshape(-1, 3)
+        cid = C.c_int32()
+        check(self.lib, self.lib.jsh_cells_upload(self.handle, A.dptr(p), A.dptr(d), p.shape[0], C.byref(cid)))
+        return cid.value
+
+    def cells_nearest(self, cells_id: int, points):
+        """Nearest cell of each point [n, 3] (cm), found on the device."""
+        p = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(p.shape[0], np.int32)
+        check(self.lib, self.lib.jsh_cells_nearest(self.handle, cells_id, A.dptr(p), p.shape[0],
+                                                   out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def random_directions(self, seed: int, keys):
+        """Random unit directions [n, 3] of the counters keys [n, 3], drawn on the device."""
+        k = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 3)
+        out = np.zeros((k.shape[0], 3))
+        check(self.lib, self.lib.jsh_random_directions(self.handle, int(seed),
+                                                       k.ctypes.data_as(C.POINTER(C.c_uint32)), k.shape[0],
+                                                       A.dptr(out)))
+        return out
+
     def grid_interpolate(self, grid_id: int, field: int, zr, nan_value=0.0):
         """Values of field `field` at points (z, r) [pc], interpolated on the device."""
         zr = np.ascontiguousarray(zr, dtype=np.float64).reshape(-1, 2)
@@ -190,6 +216,17 @@ def triangulate(xy) -> np.ndarray:
     check(lib, lib.jsh_grid_triangulate(A.dptr(xy), xy.shape[0], tri.ctypes.data_as(C.POINTER(C.c_int32)),
                                         C.byref(m)))
     return tri[:m.value].copy()
+
+
+def cells_generate(n, r_min, r_max, theta_max, exponent, seed):
+    """The cells of RandomCellsInSphere on the host (jsh_cells_generate):
+    points [n, 3] cm and unit directions [n, 3]."""
+    lib = A.load_library()
+    p = np.zeros((int(n), 3))
+    d = np.zeros((int(n), 3))
+    check(lib, lib.jsh_cells_generate(int(n), float(r_min), float(r_max), float(theta_max), float(exponent),
+                                      int(seed), A.dptr(p), A.dptr(d)))
+    return p, d
 
 
 def stats_dict(st: A.Stats) -> dict:

@@ -763,6 +763,120 @@ static double sim_value(int32_t grid, int32_t field, v3 p, double nan_value) {
 }
 
 /* ====================================================================
+ * Random directions of RandomVectorBField (src/BField.cpp:149-193) and the
+ * cells of RandomCellsInSphere (src/Cells.cpp:5-47, src/utils.cpp:249-312).
+ * The reference draws from Boost Mersenne Twisters (per OpenMP thread for
+ * PointsRandomVectorBField); the GB300 build replaces them with the
+ * counter-based Philox4x32-10 generator (Salmon et al., SC'11), restated
+ * here from the published algorithm: ten rounds of
+ *   (c0, c1, c2, c3) -> (hi(M1 c2) ^ c1 ^ k0, lo(M1 c2), hi(M0 c0) ^ c3 ^ k1, lo(M0 c0)),
+ * M0 = 0xD2511F53, M1 = 0xCD9E8D57, the key (k0, k1) advanced by
+ * (0x9E3779B9, 0xBB67AE85) between rounds.  Uniforms U = (x + 1/2) 2^-32;
+ * directions by rejection from the cube [-1, 1]^3 into the unit ball, then
+ * divided by the norm (every operation rounded once, -ffp-contract=off).
+ * Counters: a cell's direction (cell, 0xFFFFFFFF, 0, 1 << 24 | attempt), a
+ * cell's position uniforms (cell, 0xFFFFFFFE, 0, 2 << 24), the direction of
+ * one right-hand-side evaluation (pixel, frequency, evaluation index,
+ * 1 << 24 | attempt); the key is the seed.
+ * ==================================================================== */
+typedef struct { uint32_t c[4]; } jo_u4;
+
+static jo_u4 jo_philox(jo_u4 x, uint64_t seed) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    uint64_t p0 = (uint64_t)0xD2511F53u * x.c[0], p1 = (uint64_t)0xCD9E8D57u * x.c[2];
+    jo_u4 y;
+    y.c[0] = (uint32_t)(p1 >> 32) ^ x.c[1] ^ k0;
+    y.c[1] = (uint32_t)p1;
+    y.c[2] = (uint32_t)(p0 >> 32) ^ x.c[3] ^ k1;
+    y.c[3] = (uint32_t)p0;
+    x = y;
+  }
+  return x;
+}
+
+int jo_philox4x32(const uint32_t* ctr, uint64_t key, uint32_t* out) {
+  jo_u4 x = {{ctr[0], ctr[1], ctr[2], ctr[3]}};
+  jo_u4 y = jo_philox(x, key);
+  for (int i = 0; i < 4; ++i) out[i] = y.c[i];
+  return JSH_OK;
+}
+
+static double jo_u01(uint32_t x) { return ((double)x + 0.5) * 2.3283064365386962890625e-10; }
+
+void jo_random_direction(uint64_t seed, uint32_t k0, uint32_t k1, uint32_t k2, double* n) {
+  for (uint32_t a = 0; a < 64u; ++a) {
+    jo_u4 x = {{k0, k1, k2, 0x01000000u | a}};
+    jo_u4 r = jo_philox(x, seed);
+    double cx = 2.0 * jo_u01(r.c[0]) - 1.0, cy = 2.0 * jo_u01(r.c[1]) - 1.0, cz = 2.0 * jo_u01(r.c[2]) - 1.0;
+    double r2 = (cx * cx + cy * cy) + cz * cz;
+    if (r2 > 0.0 && r2 <= 1.0) {
+      double s = sqrt(r2);
+      n[0] = cx / s; n[1] = cy / s; n[2] = cz / s;
+      return;
+    }
+  }
+  n[0] = 0.0; n[1] = 0.0; n[2] = 1.0;
+}
+
+int jo_cells_generate(int64_t n, double r_min, double r_max, double theta_max, double exponent, uint64_t seed,
+                      double* points, double* dirs) {
+  if (n < 1 || !points || !dirs || exponent == 3.0) return JSH_ERR_INVALID;
+  /* generate_random_points_sphere (src/utils.cpp:267-312) */
+  double c = theta_max > 0 ? cos(theta_max) : 1.0;
+  for (int64_t j = 0; j < n; ++j) {
+    jo_u4 x = {{(uint32_t)j, 0xFFFFFFFEu, 0u, 0x02000000u}};
+    jo_u4 u = jo_philox(x, seed);
+    double r = r_min + (r_max - r_min) * jo_u01(u.c[0]);
+    double phi = 2.0 * JO_PI * jo_u01(u.c[1]);
+    double uu = (1.0 - c) * (2.0 * jo_u01(u.c[2]) - 1.0);
+    if (uu < 0.0) uu = uu - c;
+    else uu = uu + c;
+    double theta = acos(uu);
+    r = pow(r, 1. / (3.0 - exponent));
+    points[3 * j] = r * sin(theta) * cos(phi);
+    points[3 * j + 1] = r * sin(theta) * sin(phi);
+    points[3 * j + 2] = r * cos(theta);
+    /* generate_random_directions (src/utils.cpp:249-261) */
+    jo_random_direction(seed, (uint32_t)j, 0xFFFFFFFFu, 0u, dirs + 3 * j);
+  }
+  return JSH_OK;
+}
+
+#define JO_MAX_CELLS 16
+typedef struct { int used; int64_t n; double* p; double* dir; } jo_cells;
+static jo_cells g_cells[JO_MAX_CELLS];
+
+int jo_cells_register(int32_t id, const double* points, const double* dirs, int64_t n) {
+  if (id < 0 || id >= JO_MAX_CELLS || n < 1) return JSH_ERR_INVALID;
+  jo_cells* C = &g_cells[id];
+  if (C->used) { free(C->p); free(C->dir); }
+  C->p = (double*)malloc(sizeof(double) * 3 * n);
+  C->dir = (double*)malloc(sizeof(double) * 3 * n);
+  memcpy(C->p, points, sizeof(double) * 3 * n);
+  memcpy(C->dir, dirs, sizeof(double) * 3 * n);
+  C->n = n;
+  C->used = 1;
+  return JSH_OK;
+}
+
+/* RandomCells::getID (src/Cells.cpp:13-18): the smallest squared distance
+ * over every cell, the lowest index among equals. */
+int64_t jo_cells_nearest(int32_t id, const double* q) {
+  if (id < 0 || id >= JO_MAX_CELLS || !g_cells[id].used) return -1;
+  const jo_cells* C = &g_cells[id];
+  double best = INFINITY;
+  int64_t bi = 0;
+  for (int64_t i = 0; i < C->n; ++i) {
+    double dx = q[0] - C->p[3 * i], dy = q[1] - C->p[3 * i + 1], dz = q[2] - C->p[3 * i + 2];
+    double d2 = (dx * dx + dy * dy) + dz * dz;
+    if (d2 < best) { best = d2; bi = i; }
+  }
+  return bi;
+}
+
+/* ====================================================================
  * Fields: src/VField.cpp:25-274, src/BField.cpp:35-224, src/NField.cpp:5-60.
  * ==================================================================== */
 typedef struct {
@@ -1024,7 +1138,32 @@ enum { CK_I, CK_Q, CK_U, CK_V, CK_F, CK_C, CH_Q, CE_I, CE_Q, CE_U, CE_V, CN };
 /* All coefficients at a point in the lab frame: k = k'/D, eta = eta' D D,
  * with the primed quantities from the plasma-frame transforms of
  * Jet::getKI / Jet::getEtaI (src/Jet.cpp:15-46, :218-237). */
+/* RandomVectorBField::bf (src/BField.cpp:154-161): b + rnd_fraction |b| n,
+ * the wrapper's field taken in the plasma frame (VectorBField(true)). */
+static v3 brandom(const model_t* m, v3 b, v3 p, uint32_t k0, uint32_t k1, uint32_t k2) {
+  double n[3];
+  if (m->d.random.kind == JSH_RND_CELLS) {
+    double q[3] = {p.x, p.y, p.z};
+    int64_t c = jo_cells_nearest(m->d.random.cells_id, q);
+    const double* d = g_cells[m->d.random.cells_id].dir + 3 * (c < 0 ? 0 : c);
+    n[0] = d[0]; n[1] = d[1]; n[2] = d[2];
+  } else {
+    jo_random_direction(m->d.random.seed, k0, k1, k2, n);
+  }
+  double bv = vnorm(b);
+  return vadd(b, vmul(mk(n[0], n[1], n[2]), m->d.random.fraction * bv));
+}
+
+static void coefficients_key(const model_t* m, v3 p, v3 nl, double nu, int full, double* k, uint32_t rk0,
+                             uint32_t rk1, uint32_t rk2);
 static void coefficients(const model_t* m, v3 p, v3 nl, double nu, int full, double* k) {
+  coefficients_key(m, p, nl, nu, full, k, 0, 0, 0);
+}
+
+/* (rk0, rk1, rk2): pixel, frequency and evaluation index of the per-
+ * evaluation random direction (JSH_RND_POINTS). */
+static void coefficients_key(const model_t* m, v3 p, v3 nl, double nu, int full, double* k, uint32_t rk0,
+                             uint32_t rk1, uint32_t rk2) {
   v3 v = vfield(m, p);
   double gamma = getG(v);
   double D = getD(nl, v);
@@ -1046,7 +1185,9 @@ static void coefficients(const model_t* m, v3 p, v3 nl, double nu, int full, dou
     return;
   }
   v3 bl = bvector(m, p);
-  v3 b = m->d.bfield.in_plasma_frame ? bl : getBprime(bl, v);
+  int rnd = m->d.random.kind != JSH_RND_NONE;
+  if (rnd) bl = brandom(m, bl, p, rk0, rk1, rk2);
+  v3 b = (m->d.bfield.in_plasma_frame || rnd) ? bl : getBprime(bl, v);
   v3 nlp = get_n_los_prime(nl, v);
   double np = nu_p(n_prime);
   double nb = nu_b_vec(b, nlp);
@@ -1248,6 +1389,8 @@ typedef struct {
   v3 nl;        /* LOS unit vector towards the observer */
   double nu;
   int full;
+  uint32_t rk0, rk1;  /* random-direction key of the item: pixel, frequency */
+  uint32_t* ev;       /* the item's evaluation counter */
 } tctx_t;
 
 static void rhs_tau(void* c, double t, const double* x, double* dx) {
@@ -1255,7 +1398,7 @@ static void rhs_tau(void* c, double t, const double* x, double* dx) {
   tctx_t* T = (tctx_t*)c;
   v3 p = vadd(T->p0, vmul(T->dir, t));
   double k[CN];
-  coefficients(T->m, p, T->nl, T->nu, 0, k);
+  coefficients_key(T->m, p, T->nl, T->nu, 0, k, T->rk0, T->rk1, T->ev ? (*T->ev)++ : 0u);
   dx[0] = k[CK_I];
 }
 
@@ -1263,7 +1406,7 @@ static void rhs_iquv(void* c, double t, const double* x, double* dx) {
   tctx_t* T = (tctx_t*)c;
   v3 p = vadd(T->p0, vmul(T->dir, t));
   double k[CN];
-  coefficients(T->m, p, T->nl, T->nu, T->full, k);
+  coefficients_key(T->m, p, T->nl, T->nu, T->full, k, T->rk0, T->rk1, T->ev ? (*T->ev)++ : 0u);
   if (!T->full) {
     dx[0] = k[CE_I] - k[CK_I] * x[0];
     return;
@@ -1291,7 +1434,8 @@ typedef struct {
 } pix_out_t;
 
 static void render_ray(const model_t* m, v3 ro, v3 rd, v3 rd_renorm, double nu, const jsh_params* P,
-                       pix_out_t* o, jo_counters* cnt) {
+                       pix_out_t* o, jo_counters* cnt, uint32_t pix, uint32_t f) {
+  uint32_t ev = 0; /* evaluation index of the item (random-direction key) */
   memset(o, 0, sizeof(*o));
   hits_t h;
   geo_hit(&m->geo, ro, rd, &h);
@@ -1309,7 +1453,7 @@ static void render_ray(const model_t* m, v3 ro, v3 rd, v3 rd_renorm, double nu, 
     v3 pin = h.s[sidx].in, pout = h.s[sidx].out;
     double length = vnorm(vsub(pout, pin));
     double dt = length / P->n;
-    tctx_t T = {m, pin, rd, nl, nu, 0};
+    tctx_t T = {m, pin, rd, nl, nu, 0, pix, f, &ev};
     sys_t S = {rhs_tau, &T, 1, 0};
     ctl_t C = {P->tau_atol, P->tau_rtol, P->dt_max, max_steps, 0, 0, 0};
     double t = 0.0, x[NS] = {0, 0, 0, 0}, k[7][NS], x_old[NS] = {0}, k1_old[NS] = {0}, dt_used = 0.0, t_old = 0.0;
@@ -1365,7 +1509,7 @@ static void render_ray(const model_t* m, v3 ro, v3 rd, v3 rd_renorm, double nu, 
     double auto_n = P->n;
     if (background_tau > 0.1) auto_n = steps_schedule(background_tau, P->n, 10 * P->n);
     double dt = length / auto_n;
-    tctx_t T = {m, pout, nl, nl, nu, full};
+    tctx_t T = {m, pout, nl, nl, nu, full, pix, f, &ev};
     sys_t S = {rhs_iquv, &T, dim, 0};
     ctl_t C = {P->atol, P->rtol, 0.0, max_steps, 0, 0, 0};
     double t = 0.0, k[7][NS], x_old[NS], k1_old[NS], dt_used;
@@ -1418,7 +1562,7 @@ int jo_render(const jsh_model_desc* model, const jsh_plane_desc* plane, const do
     v3 ro = plane_origin(&p, (uint64_t)pix / p.n_along, (uint64_t)pix % p.n_along);
     pix_out_t o;
     jo_counters c = {0, 0, 0};
-    render_ray(&m, ro, rd, rd2, nu[f], params, &o, &c);
+    render_ray(&m, ro, rd, rd2, nu[f], params, &o, &c, (uint32_t)pix, (uint32_t)f);
     int64_t q = (int64_t)f * n_sel + sel;
     if (out->tau) out->tau[q] = o.tau;
     if (out->l) out->l[q] = o.l;
@@ -1462,7 +1606,7 @@ static double stripe_ray(const model_t* m, v3 ro, v3 rd, double nu, int n, doubl
     v3 pin = h.s[sidx].in, pout = h.s[sidx].out;
     double length = vnorm(vsub(pout, pin));
     double dt = length / n;
-    tctx_t T = {m, pin, rd, nl, nu, 0};
+    tctx_t T = {m, pin, rd, nl, nu, 0, 0, 0, NULL};
     double x = 0.0, t = 0.0, k1, k2, k4, dum = 0.0;
     int64_t step = 0;
     int found = (x >= tau_max);

@@ -92,6 +92,17 @@ int jo_hull_register(int32_t hull_id, const double* zr, int64_t n, int32_t n_cir
 /* Vertices of a registered hull's profile R(z): vz, vR [m+1] (may be NULL). */
 int jo_hull_profile(int32_t hull_id, double* vz, double* vR, int32_t* m);
 
+/* Random vector B fields (counter-based draws, see jsh_oracle.c): the
+ * Philox4x32-10 block of a counter ctr[4] and key; the random unit direction
+ * of counter (k0, k1, k2) and seed; the cells of RandomCellsInSphere; a cell
+ * set registered under id (0..15) for JSH_RND_CELLS; its nearest cell. */
+int jo_philox4x32(const uint32_t* ctr, uint64_t key, uint32_t* out);
+void jo_random_direction(uint64_t seed, uint32_t k0, uint32_t k1, uint32_t k2, double* n);
+int jo_cells_generate(int64_t n, double r_min, double r_max, double theta_max, double exponent, uint64_t seed,
+                      double* points, double* dirs);
+int jo_cells_register(int32_t id, const double* points, const double* dirs, int64_t n);
+int64_t jo_cells_nearest(int32_t id, const double* q);
+
 int jo_openmp_threads(void);
 
 #ifdef __cplusplus

@@ -68,6 +68,13 @@ def lib():
         L.jo_hull_register.argtypes = [C.c_int32, D, C.c_int64, C.c_int32]
         L.jo_hull_profile.argtypes = [C.c_int32, D, D, P(C.c_int32)]
         L.jo_openmp_threads.restype = C.c_int
+        L.jo_philox4x32.argtypes = [P(C.c_uint32), C.c_uint64, P(C.c_uint32)]
+        L.jo_random_direction.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, D]
+        L.jo_random_direction.restype = None
+        L.jo_cells_generate.argtypes = [C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint64, D, D]
+        L.jo_cells_register.argtypes = [C.c_int32, D, D, C.c_int64]
+        L.jo_cells_nearest.argtypes = [C.c_int32, D]
+        L.jo_cells_nearest.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -178,3 +185,37 @@ def hull_profile(hull_id):
 
 def threads():
     return lib().jo_openmp_threads()
+
+
+def philox4x32(ctr, key):
+    c = (C.c_uint32 * 4)(*[int(x) & 0xFFFFFFFF for x in ctr])
+    out = (C.c_uint32 * 4)()
+    _chk(lib().jo_philox4x32(c, int(key), out))
+    return [int(x) for x in out]
+
+
+def random_directions(seed, keys):
+    """Unit directions [n, 3] of the counters keys [n, 3] (k0, k1, k2)."""
+    keys = np.asarray(keys, dtype=np.uint32).reshape(-1, 3)
+    out = np.zeros((keys.shape[0], 3))
+    d = np.zeros(3)
+    for i, (a, b, c) in enumerate(keys):
+        lib().jo_random_direction(int(seed), int(a), int(b), int(c), A.dptr(d))
+        out[i] = d
+    return out
+
+
+def cells_generate(n, r_min, r_max, theta_max, exponent, seed):
+    p = np.zeros((n, 3)); d = np.zeros((n, 3))
+    _chk(lib().jo_cells_generate(n, r_min, r_max, theta_max, exponent, int(seed), A.dptr(p), A.dptr(d)))
+    return p, d
+
+
+def cells_register(cells_id, points, dirs):
+    points = np.ascontiguousarray(points, dtype=np.float64); dirs = np.ascontiguousarray(dirs, dtype=np.float64)
+    _chk(lib().jo_cells_register(cells_id, A.dptr(points), A.dptr(dirs), points.shape[0]))
+
+
+def cells_nearest(cells_id, q):
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
+    return np.array([lib().jo_cells_nearest(cells_id, A.dptr(np.ascontiguousarray(x))) for x in q], dtype=np.int64)
