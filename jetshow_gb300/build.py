@@ -4,7 +4,10 @@ nvcc compiles the kernels for sm_103a only (``-gencode
 arch=compute_103a,code=sm_103a``); g++ compiles the host translation units.
 Every unit is compiled in parallel, then nvcc links one shared library.
 Host code is built with ``-ffp-contract=off``: the image-plane constants it
-computes feed the bit-exact FP64 geometry kernels.
+computes feed the bit-exact FP64 geometry kernels.  The mixed-precision
+kernels are built with ``--fmad=false`` (no implicit fma contraction), so that
+the same lane-machine code rounds the same way in each kernel it is
+instantiated in.
 """
 from __future__ import annotations
 
@@ -23,6 +26,12 @@ LIB = os.path.join(OUT, "libjetshow_gb300.so")
 CU_SOURCES = ["jsh_kernels.cu", "jsh_fp64.cu", "jsh_persistent.cu", "jsh_noalloc.cu", "jsh_stripe.cu", "jsh_visibility.cu"]
 CPP_SOURCES = ["jsh_host.cpp", "jsh_capi.cpp", "jsh_server.cpp", "jsh_autotune.cpp", "jsh_grid.cpp", "jsh_hull.cpp", "jsh_cells.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Units whose kernels must round identically in every instantiation: the
+# mixed-precision lane machine runs in several kernels (static, single
+# persistent, split tau and IQUV kernels) whose images are bitwise equal
+# only if the compiler fuses no multiply-add on its own (the explicit fmaf
+# calls stay fused).
+NO_CONTRACT = {"jsh_persistent.cu"}
 
 
 def _cuda_home() -> str:
@@ -62,6 +71,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(OUT, src + ".o")
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                "-Xptxas", "-v", "-Xcompiler", "-fPIC,-ffp-contract=off", *inc, "-c", s, "-o", o]
+        if src in NO_CONTRACT:
+            cmd.insert(1, "--fmad=false")
         jobs.append((o, [s, *headers], cmd))
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)

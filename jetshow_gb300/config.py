@@ -6,9 +6,10 @@ Keys read (the reference file's layout):
   observation.{redshift, frequency_ghz, los_angle}
   jet.geometry: type "cone" with parameters {angle, scale_pc}
   jet.bfield: type "radial_conical" {b_1, n_b} or "spiral_conical"
-              {b_1, pitch_angle}, plus random_fraction (must be 0: the
-              per-evaluation random directions of PointsRandomVectorBField,
-              src/BField.cpp:179-192, are not provided)
+              {b_1, pitch_angle}, plus random_fraction (> 0 wraps the field
+              in PointsRandomVectorBField(bfield, random_fraction, 123) as
+              the driver does, src/main.cpp:119-126; its per-evaluation
+              directions come from the counter-based stream)
   jet.vfield: type "const_central" {gamma};  jet.nfield: type "bk" {n_1, n_n}
   image.{pixel_size_mas, number_of_pixels}
   integration.parameters.{n, tau_max, dl_max_pc, log10_tau_min, tau_n_min,
@@ -64,14 +65,16 @@ def build(cfg) -> dict:
     geometry = J.Cone((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), float(g["angle"]), float(g["scale_pc"]) * J.pc)
     b = jt["bfield"]
     bp = b["parameters"]
-    if float(bp.get("random_fraction", 0.0)) > 0.0:
-        raise NotImplementedError("random_fraction > 0 needs PointsRandomVectorBField, which is not provided")
     if b["type"] == "radial_conical":
         bfield = J.RadialConicalBField(float(bp["b_1"]), float(bp["n_b"]), True)
     elif b["type"] == "spiral_conical":
         bfield = J.SpiralConicalBField(float(bp["b_1"]), float(bp["pitch_angle"]), True)
     else:
         raise ValueError(f"bfield type {b['type']!r} is not one the config driver knows")
+    rnd = float(bp.get("random_fraction", 0.0))
+    if rnd > 0.0:
+        # as the driver: PointsRandomVectorBField(bfield, rnd_fraction, 123)
+        bfield = J.PointsRandomVectorBField(bfield, rnd, seed=123)
     v = jt["vfield"]
     if v["type"] != "const_central":
         raise ValueError(f"vfield type {v['type']!r} is not one the config driver knows (const_central)")

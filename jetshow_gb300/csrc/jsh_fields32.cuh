@@ -345,7 +345,9 @@ __device__ __forceinline__ void coef32_tail(const JshFreqConst& F, const JshMixe
   F3 cr = fcross(nlp, B);
   float w = sqrtf(fdot(cr, cr)) * D;
   float P = 0.f, Rw = 0.f;
-  if (w > 0.f) {
+  // w = 0 (no field across the line of sight) gives zero coefficients; a
+  // NaN field (a law undefined at the point) propagates as in the reference
+  if (!(w <= 0.f)) {
     P = fpow(w, X.pk);
     Rw = P * rsqrtf(w);
   }

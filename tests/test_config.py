@@ -54,11 +54,16 @@ def test_config_builds_the_drivers_observation(lib, tmp_path):
         assert jy == pytest.approx(1e-23 / (0.002 * J.mas_to_rad) ** 2)
 
 
+def test_config_random_fraction_wraps_the_field(lib):
+    # the driver's PointsRandomVectorBField(bfield, random_fraction, 123)
+    cfg = json.loads(json.dumps(CFG))
+    cfg["jet"]["bfield"]["parameters"]["random_fraction"] = 0.3
+    d = CF.build(cfg)["jet"].desc()
+    assert (d.random.kind, d.random.fraction, d.random.seed) == (A.RND_POINTS, 0.3, 123)
+    assert d.bfield.kind == A.B_SPIRAL_CONICAL
+
+
 def test_config_rejects_what_the_driver_cannot_render(lib):
-    bad = json.loads(json.dumps(CFG))
-    bad["jet"]["bfield"]["parameters"]["random_fraction"] = 0.3
-    with pytest.raises(NotImplementedError):
-        CF.build(bad)
     bad = json.loads(json.dumps(CFG))
     bad["jet"]["geometry"]["type"] = "cylinder"
     with pytest.raises(ValueError):

@@ -59,15 +59,15 @@ def test_interpolation_reproduces_linear_field(ctx):
 # implementations of the same FP64 algorithm are compared at GRID_TIGHT_KW
 # (a last-bit difference moves the adaptive steps across the kinks; at these
 # tolerances the two images stay within 1e-6 of each other), on a short jet
-# bounded by the hull of the grid points with 0.5 <= z <= 3 pc (one thread
-# per item on the FP64 pipe: the cost of the heaviest ray sets the test's
-# time).  The mixed path is compared with a converged solution at
+# bounded by the hull of the grid points with 1 <= z <= 2 pc and r <= 0.1 pc
+# (one thread per item on the FP64 pipe, the lanes of a warp diverging: the
+# heaviest ray sets the test's time).  The mixed path is compared with a converged solution at
 # GRID_MIXED_KW.  Every gate is the contract's.
 
 
 def short_jet(ctx, oracle, c3, scale):
     gid, xy, _, _ = c3
-    inner = xy[(xy[:, 0] >= 0.5) & (xy[:, 0] <= 3.0) & (xy[:, 1] <= 0.25)]
+    inner = xy[(xy[:, 0] >= 1.0) & (xy[:, 0] <= 2.0) & (xy[:, 1] <= 0.1)]
     hid = ctx.hull_upload(inner, 36)
     oracle.hull_register(hid, inner, 36)
     jet, plane, nu, _ = W.simulation_c3(gid, scale=scale)

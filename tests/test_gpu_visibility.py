@@ -41,7 +41,7 @@ def test_visibilities_match_direct_sum(ctx, case):
     pcm = W.pc_per_mas()
     rad_per_cm = MAS_TO_RAD / (pcm * J.pc)
     jy = 1e23 / (1 + W.Z) ** 3 * rad_per_cm ** 2
-    uv = uv_points(1500, 5e8)
+    uv = uv_points(1500, 2e9)
     dx, dy, rot = 0.3 * MAS_TO_RAD, -0.2 * MAS_TO_RAD, 0.7
     vis, st = ctx.visibilities(jet.desc(), plane.desc(), nu, p, uv, rad_per_cm, jy, dx, dy, rot)
     assert vis.shape == (nu.size, uv.shape[0])
@@ -56,8 +56,9 @@ def test_visibilities_match_direct_sum(ctx, case):
         assert np.max(np.abs(vis[f] - ref)) < 1e-6 * np.max(np.abs(ref))
         # zero spacing: the total flux density of the image
         assert abs(vis[f][0] - (img["I"][f] * flux_w).sum()) < 1e-6 * abs(vis[f][0])
-        # the longest baselines turn the phase across the image by hundreds of cycles
-        assert 5e8 * np.ptp(along) * rad_per_cm > 30 or case == "c0_uniform"
+        # the longest baselines turn the phase across the image by tens to
+        # hundreds of cycles
+        assert 2e9 * np.ptp(along) * rad_per_cm > 25
 
 
 def test_get_i_visibilities_drop_in(ctx):
