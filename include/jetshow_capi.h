@@ -258,10 +258,12 @@ typedef struct jsh_params {
  * items that need the second pass, ranked by the optical depth it crosses).
  * Results are bitwise the same; the flag exists for comparison. */
 #define JSH_FLAG_SINGLE_KERNEL 0x8
-/* Split form: launch the tau kernel's build bounded to 85 registers (24
- * resident warps per SM, a few spills) instead of the 128-register one.
- * Results are bitwise the same. */
-#define JSH_FLAG_TAU_DENSE 0x10
+/* Split form: launch the kernels built for every field law even when the
+ * model is of the benchmark family (helical conical B and BK n in the plasma
+ * frame, ConstFlat V), whose requests otherwise run kernels compiled with
+ * that family's fused coefficient path alone (fewer registers, more
+ * resident warps).  Results are bitwise the same; for comparison. */
+#define JSH_FLAG_GENERAL_KERNELS 0x10
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,

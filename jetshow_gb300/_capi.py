@@ -33,7 +33,7 @@ FLAG_IQUV_FROM_TAU_MAX = 0x1
 FLAG_COST_MAP = 0x2
 FLAG_COMPACT_REGS = 0x4
 FLAG_SINGLE_KERNEL = 0x8
-FLAG_TAU_DENSE = 0x10
+FLAG_GENERAL_KERNELS = 0x10
 ST_ERRORS = ST_STEP_LIMIT | ST_FAIL_LIMIT | ST_BISECT_LIMIT | ST_NAN | ST_DT_UNDERFLOW
 
 GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE, GEO_SIMULATION = 1, 2, 3, 4, 5

@@ -143,7 +143,6 @@ JshLaunchShape jsh_params_shape(JshLaunchShape s, const jsh_params* params) {
   if (params->refill_threshold > 0) s.refill_threshold = params->refill_threshold;
   if (params->flags & JSH_FLAG_COMPACT_REGS) s.compact = 1;
   if (params->flags & JSH_FLAG_SINGLE_KERNEL) s.single = 1;
-  if (params->flags & JSH_FLAG_TAU_DENSE) s.tau_dense = 1;
   if (s.block_size < 32) s.block_size = 32;
   if (s.block_size > 512) s.block_size = 512;
   s.block_size = s.block_size / 32 * 32;
@@ -363,6 +362,7 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
   JSH_CUDA_TRY(jsh_launch_plane(d_req, 1, plane->n_along, stream));
   JSH_CUDA_TRY(jsh_launch_hit(d_req, 1, npix, stream));
   JshLaunchShape shape = jsh_effective_shape(ctx, params);
+  shape.fused = (req.mix.helical_log && !(params->flags & JSH_FLAG_GENERAL_KERNELS)) ? 1 : 0;
   JSH_CUDA_TRY(jsh_launch_transfer(d_req, 1, params->precision, params->schedule, params->output == JSH_OUT_FULL,
                                    npix * (uint64_t)n_nu, npix, shape, (unsigned int*)(base + L.off_queue),
                                    ctx->num_sms, stream));

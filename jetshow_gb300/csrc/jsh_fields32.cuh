@@ -133,10 +133,22 @@ __device__ inline Vel vfield32(const JshModel& m, const JshMixed& X, F3 p) {
       return Vel{g, a * rsqrtf(fdot(a, a))};
     }
     case JSH_V_SHEATH_CENTRAL: {
+      // theta = acos(z / |p + o|) < theta_sheath (src/VField.cpp): near a
+      // small sheath angle acos in FP32 is ill-conditioned (1 - cos theta
+      // ~ 2e-4 at 0.02 rad magnifies the rounding of z / r by 1/theta^2), so
+      // for z > 0 the test compares 1 - cos theta = (|a|^2 - z^2) / (r (r + z)),
+      // a = p + o, formed without cancellation, with 1 - cos theta_sheath
       F3 a = p + f3(q[3], q[4], q[5]) * inv_pc;
       float r = sqrtf(fdot(a, a));
-      float theta = acosf(p.z / r);
-      return Vel{theta < q[2] ? q[0] : q[1], a * (1.f / r)};
+      bool spine;
+      if (p.z > 0.f) {
+        const float oz = q[5] * inv_pc;
+        const float num = fmaf(a.x, a.x, fmaf(a.y, a.y, oz * (2.f * p.z + oz)));
+        spine = num / (r * (r + p.z)) < X.v_omc;
+      } else {
+        spine = acosf(p.z / r) < q[2];
+      }
+      return Vel{spine ? q[0] : q[1], a * (1.f / r)};
     }
     case JSH_V_CONST_PARABOLIC: return Vel{q[0], parabolic_dir(qp[1], p)};
     case JSH_V_ACC_PARABOLIC: {
@@ -419,11 +431,15 @@ __device__ __forceinline__ void coef32_helical_log(const JshMixed& X, const JshF
 
 // (rk_h, rk_f, rk_e): hit index, frequency and evaluation index of the
 // per-evaluation random direction (JSH_RND_POINTS only).
+// GENERAL = false compiles the fused benchmark-family path alone, for
+// kernels launched only on requests whose mix.helical_log is set (the same
+// arithmetic as the general build takes for them).
+template <bool GENERAL = true>
 __device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqConst& F, F3 p, int mode, Coef32& c,
                                           uint32_t rk_h = 0, uint32_t rk_f = 0, uint32_t rk_e = 0) {
   const JshModel& m = R.model;
   const JshMixed& X = R.mix;
-  if (X.helical_log) {
+  if (!GENERAL || X.helical_log) {
     coef32_helical_log(X, F, p, mode, c);
     return;
   }

@@ -15,7 +15,8 @@ struct JshLaunchShape {
   int refill_threshold;  // persistent schedule: refill when >= this many lanes idle
   int compact;           // mixed persistent schedule: the 168-register build (<= 128 threads)
   int single;            // mixed persistent schedule: tau and IQUV passes in one kernel (else split)
-  int tau_dense;         // split form: the tau kernel's 85-register build (24 warps per SM)
+  int fused;             // split form: every request of the batch is of the fused benchmark
+                         // family (mix.helical_log): launch the kernels built for it alone
 };
 
 // Ray generation: along sizes and centres (sequential recurrence of

@@ -181,7 +181,8 @@ extern "C" int jsh_observation_run_noalloc(const jsh_model_desc* model, const js
   const JshRequest* d_req = (const JshRequest*)(base + L.off_req);
   JSH_CUDA_TRY(jsh_launch_plane(d_req, 1, plane->n_along, s));
   JSH_CUDA_TRY(jsh_launch_hit(d_req, 1, npix, s));
-  const JshLaunchShape shape = jsh_params_shape(JshLaunchShape{128, 0, 8, 0}, params);
+  JshLaunchShape shape = jsh_params_shape(JshLaunchShape{128, 0, 8, 0}, params);
+  shape.fused = (in.req.mix.helical_log && !(params->flags & JSH_FLAG_GENERAL_KERNELS)) ? 1 : 0;
   JSH_CUDA_TRY(jsh_launch_transfer(d_req, 1, params->precision, params->schedule, params->output == JSH_OUT_FULL,
                                    npix * (uint64_t)n_nu, npix, shape, (unsigned int*)(base + L.off_queue), sms, s));
   return JSH_OK;

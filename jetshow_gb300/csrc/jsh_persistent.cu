@@ -415,11 +415,12 @@ __device__ __noinline__ double crossing_time(double tau_old, double t_old, doubl
 // (every active lane of the warp in its tau pass) after k_I.  Returns the
 // magnitude of the terms summed into the derivatives (eta_I + k_I |I| for
 // the Stokes vector, k_I for tau): the scale of their FP32 rounding noise.
+template <bool GENERAL>
 __device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& F, bool tau, bool full, bool kionly,
                                        F3 p, const float* y, float cs, float sn, float* dk, float& kI, uint32_t rk_h,
                                        uint32_t rk_f, uint32_t rk_e) {
   Coef32 c;
-  coef32_rt(R, F, p, kionly ? COEF_KI : (full ? COEF_FULL : COEF_I), c, rk_h, rk_f, rk_e);
+  coef32_rt<GENERAL>(R, F, p, kionly ? COEF_KI : (full ? COEF_FULL : COEF_I), c, rk_h, rk_f, rk_e);
   kI = c.kI;
   if (tau) {
     dk[0] = c.kI;
@@ -551,7 +552,7 @@ struct StageWidth {
 // needing an I/IQUV pass is emitted at the transition; PASS_IQUV: lanes
 // start in their IQUV pass); the arithmetic of each pass is the same in
 // every form, so the images are bitwise the same.
-template <bool FULL, int PASS>
+template <bool FULL, int PASS, bool GENERAL = true>
 __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict__ reqs, bool warp_tau,
                                           const Stages<StageWidth<FULL, PASS>::NK>& K) {
   constexpr int NK = StageWidth<FULL, PASS>::NK;
@@ -598,7 +599,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     const float h = L.dt;
     float dk[5];
     if (!L.init) {
-      L.s1 = rhs32(R, F, tau, coef_full, tau && warp_tau, pn, L.x, c0, s0, dk, L.kI1, L.h, (uint32_t)L.f,
+      L.s1 = rhs32<GENERAL>(R, F, tau, coef_full, tau && warp_tau, pn, L.x, c0, s0, dk, L.kI1, L.h, (uint32_t)L.f,
                    L.evals0 + L.evals);
 #pragma unroll
       for (int c = 0; c < NK; ++c) L.k1[c] = dk[c];
@@ -623,7 +624,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
         cs = c0 * cd - s0 * sd;
         sn = s0 * cd + c0 * sd;
       }
-      const float sc = rhs32(R, F, tau, coef_full, tau && warp_tau, pn + dirf * (c_C[s] * h), y, cs, sn, dk, kI7,
+      const float sc = rhs32<GENERAL>(R, F, tau, coef_full, tau && warp_tau, pn + dirf * (c_C[s] * h), y, cs, sn, dk, kI7,
                              L.h, (uint32_t)L.f, L.evals0 + L.evals + (uint32_t)(s - 1));
       smax = fmaxf(smax, sc);
       s7 = sc;
@@ -993,11 +994,12 @@ __global__ void __launch_bounds__(COMPACT ? 128 : 256, COMPACT ? 3 : 1)
 
 // Tau kernel: persistent CTAs, lanes refilled from the ranked queue (the
 // same order as the single-kernel form), each item's tau pass to its end.
-// MINB resident 256-thread CTAs per SM bound its registers: 2 (at most 128,
-// no spills) or 3 (at most 85, a few spills, 24 warps per SM).
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) transfer_tau_kernel(const JshRequest* __restrict__ reqs, int n_req,
-                                                              unsigned long long* queue, int refill) {
+// GENERAL = false: the build for batches of the fused benchmark family
+// alone (80 registers, 24 resident warps per SM, against 128 and 16).
+template <bool GENERAL>
+__global__ void __launch_bounds__(256, GENERAL ? 2 : 3) transfer_tau_kernel(const JshRequest* __restrict__ reqs,
+                                                                          int n_req, unsigned long long* queue,
+                                                                          int refill) {
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
   extern __shared__ float ksh[];
   batch_prefix(reqs, n_req, base);
@@ -1026,7 +1028,7 @@ __global__ void __launch_bounds__(256, MINB) transfer_tau_kernel(const JshReques
       if (exhausted) break;
       continue;
     }
-    if (L.phase != PH_IDLE) lane_step<false, PASS_TAU>(L, reqs, true, K);
+    if (L.phase != PH_IDLE) lane_step<false, PASS_TAU, GENERAL>(L, reqs, true, K);
   }
 }
 
@@ -1088,7 +1090,7 @@ __device__ __forceinline__ void iquv_prefix(const JshRequest* __restrict__ reqs,
 
 // IQUV kernel: persistent CTAs over the ranked emitted items (COMPACT: the
 // register-capped build, as for the single-kernel form).
-template <bool FULL, bool COMPACT>
+template <bool FULL, bool COMPACT, bool GENERAL>
 __global__ void __launch_bounds__(COMPACT ? 128 : 256, COMPACT ? 3 : 1)
     transfer_iquv_kernel(const JshRequest* __restrict__ reqs, int n_req, unsigned long long* queue, int refill) {
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
@@ -1119,7 +1121,7 @@ __global__ void __launch_bounds__(COMPACT ? 128 : 256, COMPACT ? 3 : 1)
       if (exhausted) break;
       continue;
     }
-    if (L.phase != PH_IDLE) lane_step<FULL, PASS_IQUV>(L, reqs, false, K);
+    if (L.phase != PH_IDLE) lane_step<FULL, PASS_IQUV, GENERAL>(L, reqs, false, K);
   }
 }
 
@@ -1135,12 +1137,13 @@ int occupancy_mixed(bool split, bool full, int block_size, bool compact) {
   const size_t sm = full ? stage_smem<true>(block_size) : stage_smem<false>(block_size);
 #define JSH_OCC(kernel) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block_size, sm)
   if (split) {
+    // the general build bounds both (it holds at least the fused one's registers)
     if (compact) {
-      if (full) JSH_OCC((transfer_iquv_kernel<true, true>));
-      else JSH_OCC((transfer_iquv_kernel<false, true>));
+      if (full) JSH_OCC((transfer_iquv_kernel<true, true, true>));
+      else JSH_OCC((transfer_iquv_kernel<false, true, true>));
     } else {
-      if (full) JSH_OCC((transfer_iquv_kernel<true, false>));
-      else JSH_OCC((transfer_iquv_kernel<false, false>));
+      if (full) JSH_OCC((transfer_iquv_kernel<true, false, true>));
+      else JSH_OCC((transfer_iquv_kernel<false, false, true>));
     }
   } else {
     if (compact) {
@@ -1187,18 +1190,18 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
     // tau kernel: 256 threads, every CTA it can keep resident
     const int bt = 256;
     int per_sm_t = 0;
-    if (shape.tau_dense)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_t, transfer_tau_kernel<3>, bt, stage_smem<false>(bt));
+    if (shape.fused)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_t, transfer_tau_kernel<false>, bt, stage_smem<false>(bt));
     else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_t, transfer_tau_kernel<2>, bt, stage_smem<false>(bt));
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_t, transfer_tau_kernel<true>, bt, stage_smem<false>(bt));
     if (per_sm_t < 1) per_sm_t = 1;
     unsigned bl_t = (unsigned)(num_sms * per_sm_t);
     if ((uint64_t)bl_t * bt > need) bl_t = (unsigned)((need + bt - 1) / bt);
     if (bl_t == 0) bl_t = 1;
-    if (shape.tau_dense)
-      transfer_tau_kernel<3><<<bl_t, bt, stage_smem<false>(bt), stream>>>(d_reqs, n_req, q, rf);
+    if (shape.fused)
+      transfer_tau_kernel<false><<<bl_t, bt, stage_smem<false>(bt), stream>>>(d_reqs, n_req, q, rf);
     else
-      transfer_tau_kernel<2><<<bl_t, bt, stage_smem<false>(bt), stream>>>(d_reqs, n_req, q, rf);
+      transfer_tau_kernel<true><<<bl_t, bt, stage_smem<false>(bt), stream>>>(d_reqs, n_req, q, rf);
     const dim3 gi((unsigned)num_sms, (unsigned)n_req);
     iquv_hist_kernel<<<gi, 256, 0, stream>>>(d_reqs);
     iquv_prefix_kernel<<<n_req, 32, 0, stream>>>(d_reqs);
@@ -1213,13 +1216,23 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
   if (blocks == 0) blocks = 1;
   const size_t smem = full ? stage_smem<true>(bs) : stage_smem<false>(bs);
   if (split) {
-    if (shape.compact) {
-      if (full) transfer_iquv_kernel<true, true><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf);
-      else transfer_iquv_kernel<false, true><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf);
+#define JSH_IQUV(F, CP, G) transfer_iquv_kernel<F, CP, G><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf)
+    if (shape.fused) {
+      if (shape.compact) {
+        if (full) JSH_IQUV(true, true, false);
+        else JSH_IQUV(false, true, false);
+      } else {
+        if (full) JSH_IQUV(true, false, false);
+        else JSH_IQUV(false, false, false);
+      }
+    } else if (shape.compact) {
+      if (full) JSH_IQUV(true, true, true);
+      else JSH_IQUV(false, true, true);
     } else {
-      if (full) transfer_iquv_kernel<true, false><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf);
-      else transfer_iquv_kernel<false, false><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q + 1, rf);
+      if (full) JSH_IQUV(true, false, true);
+      else JSH_IQUV(false, false, true);
     }
+#undef JSH_IQUV
   } else if (shape.compact) {
     if (full) transfer_persistent_mixed_kernel<true, true><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q, rf);
     else transfer_persistent_mixed_kernel<false, true><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q, rf);
@@ -1285,6 +1298,7 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   X.v_cone_oz = (float)m.v_cone_oz;
   X.v_cone_oz_pc = (float)(m.v_cone_oz / JSH_PC);
   X.v_theta = (float)m.v_theta;
+  X.v_omc = (float)(2.0 * sin(0.5 * m.vp[2]) * sin(0.5 * m.vp[2]));
   X.sin_pitch = (float)m.sin_pitch;
   X.cos_pitch = (float)m.cos_pitch;
   X.tan_pitch = (float)m.tan_pitch;

@@ -76,6 +76,7 @@ struct JshMixed {
   // constants the FP32 field laws use: no FP64 operation per evaluation
   float vq[8], vq_pc[8], nq[8], nq_pc[8], bq[8], bq_pc[8];
   float v_dq01, v_g0m1, v_cone_oz, v_cone_oz_pc, v_theta;
+  float v_omc;           // SheathCentral: 1 - cos(theta_sheath) = 2 sin^2(theta_sheath / 2)
   float sin_pitch, cos_pitch, tan_pitch, b_bessel0, b_bessel1;
   float tau_atol, tau_rtol, rtol;  // FP32 copies of the step-control tolerances
   float dt_max_f;                  // dt_max_pc in FP32

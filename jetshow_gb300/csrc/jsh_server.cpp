@@ -126,7 +126,8 @@ struct Slot {
   unsigned long long* h_counters = nullptr;  // pinned [JSH_MAX_BATCH][8], written by the batch's last copy
   char* dev = nullptr;       // device control block: SlotHost image + counters region
   size_t counters_off = 0, counters_bytes = 0;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // I-only, full Stokes
+  // [output kind: I-only, full Stokes][kernels: general, fused benchmark family]
+  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   bool busy = false;
   std::vector<Request*> batch;
   int n_req = 0;
@@ -224,7 +225,7 @@ void bind_empty(Slot& sl, int i) {
 }
 
 // Enqueue (or capture) the launch sequence of slot `sl` for `n_req` records.
-cudaError_t enqueue_slot(jsh_server* S, Slot& sl, int n_req, bool full) {
+cudaError_t enqueue_slot(jsh_server* S, Slot& sl, int n_req, bool full, bool fused) {
   cudaStream_t st = sl.stream;
   const JshRequest* d_recs = (const JshRequest*)sl.dev;
   cudaError_t e = cudaMemcpyAsync(sl.dev, sl.host, sizeof(SlotHost), cudaMemcpyHostToDevice, st);
@@ -236,6 +237,7 @@ cudaError_t enqueue_slot(jsh_server* S, Slot& sl, int n_req, bool full) {
   e = jsh_launch_hit(d_recs, n_req, S->cap_pix, st);
   if (e != cudaSuccess) return e;
   JshLaunchShape shape = S->ctx->shape;
+  shape.fused = fused ? 1 : 0;
   unsigned int* queue = (unsigned int*)(sl.dev + sl.counters_off + sl.counters_bytes - 256);
   e = jsh_launch_transfer(d_recs, n_req, S->cfg.precision, JSH_SCHED_PERSISTENT, full,
                           S->cap_pix * (uint64_t)S->cap_nu * (uint64_t)n_req, S->cap_pix, shape, queue,
@@ -252,15 +254,15 @@ namespace {
 // Capture the launch sequence of slot `sl` for one output kind into a graph.
 // The records are read from the control block when the graph runs, so one
 // graph per (slot, output kind) serves every batch.
-cudaError_t build_graph(jsh_server* S, Slot& sl, bool full) {
+cudaError_t build_graph(jsh_server* S, Slot& sl, bool full, bool fused) {
   cudaGraph_t g;
   cudaError_t e = cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
-  e = enqueue_slot(S, sl, S->cfg.max_batch_requests, full);
+  e = enqueue_slot(S, sl, S->cfg.max_batch_requests, full, fused);
   cudaError_t e2 = cudaStreamEndCapture(sl.stream, &g);
   if (e != cudaSuccess) return e;
   if (e2 != cudaSuccess) return e2;
-  e = cudaGraphInstantiate(&sl.graph[full ? 1 : 0], g, 0);
+  e = cudaGraphInstantiate(&sl.graph[full ? 1 : 0][fused ? 1 : 0], g, 0);
   cudaGraphDestroy(g);
   return e;
 }
@@ -272,11 +274,15 @@ int launch_batch(jsh_server* S, Slot& sl) {
   const int cap = S->cfg.max_batch_requests;
   for (int i = n; i < cap; ++i) bind_empty(sl, i);
   const bool full = sl.batch[0]->params.output == JSH_OUT_FULL;
+  // the fused kernels serve a batch whose every request is of the benchmark family
+  bool fused = S->cfg.precision == JSH_PREC_MIXED;
+  for (int i = 0; i < n && fused; ++i)
+    fused = sl.batch[i]->rec.mix.helical_log && !(sl.batch[i]->params.flags & JSH_FLAG_GENERAL_KERNELS);
   cudaError_t e;
   if (S->cfg.use_graphs)
-    e = cudaGraphLaunch(sl.graph[full ? 1 : 0], sl.stream);
+    e = cudaGraphLaunch(sl.graph[full ? 1 : 0][fused ? 1 : 0], sl.stream);
   else
-    e = enqueue_slot(S, sl, cap, full);
+    e = enqueue_slot(S, sl, cap, full, fused);
   if (e != cudaSuccess) goto fail;
   e = cudaEventRecord(sl.done, sl.stream);
   if (e != cudaSuccess) goto fail;
@@ -416,8 +422,8 @@ extern "C" int jsh_server_create(jsh_ctx* ctx, const jsh_server_config* cfg, jsh
     sl.counters_bytes = counters_region_bytes();
     memset(sl.host, 0, sizeof(SlotHost));
     if (cfg->use_graphs) {
-      cudaError_t e = build_graph(S, sl, false);
-      if (e == cudaSuccess) e = build_graph(S, sl, true);
+      cudaError_t e = cudaSuccess;
+      for (int fk = 0; fk < 4 && e == cudaSuccess; ++fk) e = build_graph(S, sl, (fk & 1) != 0, (fk & 2) != 0);
       if (e != cudaSuccess) {
         jsh_set_error("server graph capture failed: %s", cudaGetErrorString(e));
         S->stop = true;
@@ -450,8 +456,9 @@ extern "C" void jsh_server_destroy(jsh_server* S) {
   cudaSetDevice(S->ctx->device);
   for (auto& sl : S->slots) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
-    for (auto g : sl.graph)
-      if (g) cudaGraphExecDestroy(g);
+    for (auto& row : sl.graph)
+      for (auto g : row)
+        if (g) cudaGraphExecDestroy(g);
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.stream) cudaStreamDestroy(sl.stream);
     if (sl.host) cudaFreeHost(sl.host);

@@ -122,7 +122,7 @@ def test_cost_map_counts_every_evaluation(ctx):
 
 
 @pytest.mark.parametrize("output", ["full", "I"])
-@pytest.mark.parametrize("flags", [A.FLAG_SINGLE_KERNEL, A.FLAG_TAU_DENSE, A.FLAG_COMPACT_REGS,
+@pytest.mark.parametrize("flags", [A.FLAG_SINGLE_KERNEL, A.FLAG_GENERAL_KERNELS, A.FLAG_COMPACT_REGS,
                                    A.FLAG_IQUV_FROM_TAU_MAX])
 def test_split_kernels_match_single_kernel(ctx, flags, output):
     """The persistent schedule's split form (a tau kernel, then an IQUV kernel
