@@ -53,13 +53,13 @@ CENSUS_FP32_INSTR = 116
 CENSUS_MUFU = 12
 CENSUS_TAU_FP32_INSTR = 55
 CENSUS_TAU_MUFU = 5
-# DRAM bytes (read + write) of one transfer launch: the ncu capture of the
-# 256x512 render (206 368 items, 6.12 MB read + 6.9 KB written: the hit list
-# and request records; the output planes stay in the 129 MB L2 during the
-# launch) scaled by the full render's 4.004x hit rays
-TRAFFIC_BYTES_PER_LAUNCH = int(round((6123264 + 6912) * 826336 / 206368))
-TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one transfer launch on the 256x512 "
-                  "render (206 368 items), scaled by the hit rays")
+# DRAM bytes (read + write) per launch of the two transfer kernels of the
+# split form, from an ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum) of the 256x512 render scaled to the full render by
+# its hit rays; None until captured for this build
+TRAFFIC_BYTES_PER_LAUNCH = {"transfer_tau_kernel": None, "transfer_iquv_kernel": None}
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of each transfer kernel on the "
+                  "256x512 render, scaled by the hit rays")
 
 
 def parse():
@@ -397,7 +397,10 @@ class Renderer:
         self.ptrs = {k: v.data_ptr() for k, v in self.planes.items()}
         self.flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    def timed(self, model, pdesc, nu, params, steps, warmup):
+    def timed(self, model, pdesc, nu, params, steps, warmup, kernel_ms=None):
+        """Device time [ms] of each timed step; with ``kernel_ms`` (a list)
+        the request's per-kernel times of each timed step are appended to it
+        (params carry FLAG_KERNEL_TIMES)."""
         torch = self.torch
         ms = []
         for i in range(warmup + steps):
@@ -411,6 +414,8 @@ class Renderer:
             self.stream.synchronize()
             if i >= warmup:
                 ms.append(e0.elapsed_time(e1))
+                if kernel_ms is not None:
+                    kernel_ms.append(self.ctx.last_kernel_ms())
         return ms, self.ctx.last_stats()
 
     def host(self, n_nu, npix):
@@ -480,7 +485,7 @@ def main():
 
     kw_cfg = dict(kw)
     kw = dict(W.ACCURATE_KW)  # every form at the 1e-4-qualified tolerances
-    p_batched = J.make_params(precision="mixed", schedule="persistent", **kw)
+    p_batched = J.make_params(precision="mixed", schedule="persistent", flags=A.FLAG_KERNEL_TIMES, **kw)
     p_mixed = J.make_params(precision="mixed", schedule="static", **kw)
     p_plain = J.make_params(precision="fp64", schedule="static", **kw)
     p_cfg = J.make_params(precision="mixed", schedule="persistent", **kw_cfg)
@@ -490,15 +495,17 @@ def main():
     if args.shape:
         b, c, r, k = (int(x) for x in args.shape.split(","))
         p_batched = J.make_params(precision="mixed", schedule="persistent", block_size=b, ctas_per_sm=c,
-                                  refill_threshold=r, flags=A.FLAG_COMPACT_REGS if k else 0, **kw)
+                                  refill_threshold=r, flags=A.FLAG_KERNEL_TIMES | (A.FLAG_COMPACT_REGS if k else 0),
+                                  **kw)
         tuning = {"block_size": b, "ctas_per_sm": c, "refill_threshold": r, "compact": k, "ms": None,
                   "fixed": True}
     else:
         tuning = ctx.autotune(model, pdesc, nu, p_batched)
     p_tmax = J.make_params(precision="mixed", schedule="persistent", flags=A.FLAG_IQUV_FROM_TAU_MAX, **kw)
     barrier()
+    kms = []
     with ClockSampler(local) as clk:
-        ms_b, st_b = R.timed(model, pdesc, nu, p_batched, args.steps, args.warmup)
+        ms_b, st_b = R.timed(model, pdesc, nu, p_batched, args.steps, args.warmup, kernel_ms=kms)
     barrier()
     items = st_b["n_work_items"]
     out_b = R.host(nu.size, npix)
@@ -544,7 +551,10 @@ def main():
     d2h = sum(v.numel() * v.element_size() for v in host.values())
     h2d = int(ctx.lib.jsh_request_h2d_bytes(nu_c.size, A.PREC_MIXED))
 
-    # ---- roofline of the dominant kernel (persistent transfer)
+    # ---- roofline of the dominant kernel: the split form's tau kernel or
+    # IQUV kernel, each timed live with CUDA events on the launching stream
+    # over the timed steps; the algorithmic work is the source-level census
+    # per right-hand-side evaluation times the kernel's evaluations
     peaks = ctx.device_peaks()
     # tau-pass evaluations of a render: the same request with the IQUV pass
     # switched off (tau_min above every depth; the tau pass is unchanged)
@@ -553,21 +563,33 @@ def main():
     n_tau = min(st_tau["rhs_evals"], st_b["rhs_evals"])
     n_iquv = st_b["rhs_evals"] - n_tau
     sec = t_step * 1e-3
+    tau_ms = float(np.mean([k["tau_ms"] for k in kms]))
+    rank_ms = float(np.mean([k["iquv_rank_ms"] for k in kms]))
+    iquv_ms = float(np.mean([k["iquv_ms"] for k in kms]))
+    kernels = {}
+    for name, n_ev, instr, mufu, ms_k in (("transfer_tau_kernel", n_tau, CENSUS_TAU_FP32_INSTR, CENSUS_TAU_MUFU, tau_ms),
+                                          ("transfer_iquv_kernel", n_iquv, CENSUS_FP32_INSTR, CENSUS_MUFU, iquv_ms)):
+        ach = n_ev * instr * 2 / (ms_k * 1e-3) / 1e12
+        kernels[name] = {"ms": ms_k, "rhs_evals": int(n_ev), "achieved": ach, "frac": ach / peaks["fp32_tflops"],
+                         "mufu_frac": n_ev * mufu / (ms_k * 1e-3) / 1e12 / peaks["mufu_tops"],
+                         "share_of_step": ms_k / t_step}
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
     evals_per_s = st_b["rhs_evals"] / sec
     fp32_instr = n_tau * CENSUS_TAU_FP32_INSTR + n_iquv * CENSUS_FP32_INSTR
     mufu_ops = n_tau * CENSUS_TAU_MUFU + n_iquv * CENSUS_MUFU
-    achieved = fp32_instr * 2 / sec / 1e12
-    roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
-            "frac": achieved / peaks["fp32_tflops"], "traffic": TRAFFIC_BYTES_PER_LAUNCH,
+    render_achieved = fp32_instr * 2 / sec / 1e12
+    roof = {"bound": "fp32", "kernel": dom, "achieved": kernels[dom]["achieved"], "peak": peaks["fp32_tflops"],
+            "unit": "TFLOP/s", "frac": kernels[dom]["frac"], "traffic": TRAFFIC_BYTES_PER_LAUNCH.get(dom),
             "traffic_source": TRAFFIC_SOURCE,
             "peak_source": "measured FMA-chain microbenchmark on this GPU in this run (MEASURED_PEAKS.json "
                            "holds only HBM and bf16 peaks)",
+            "kernels": kernels, "iquv_rank_ms": rank_ms,
+            "render": {"achieved": render_achieved, "frac": render_achieved / peaks["fp32_tflops"],
+                       "ms": t_step, "rhs_evals_per_s": evals_per_s,
+                       "mufu_frac": mufu_ops / sec / 1e12 / peaks["mufu_tops"]},
             "census": {"fp32_instr_per_rhs": CENSUS_FP32_INSTR, "mufu_per_rhs": CENSUS_MUFU,
                        "fp32_instr_per_tau_rhs": CENSUS_TAU_FP32_INSTR, "mufu_per_tau_rhs": CENSUS_TAU_MUFU,
                        "tau_evals_per_step": int(n_tau), "iquv_evals_per_step": int(n_iquv)},
-            "rhs_evals_per_s": evals_per_s,
-            "mufu": {"achieved_tops": mufu_ops / sec / 1e12, "peak_tops": peaks["mufu_tops"],
-                     "frac": mufu_ops / sec / 1e12 / peaks["mufu_tops"]},
             "fp64_peak_tflops": peaks["fp64_tflops"]}
     cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 and conical else None
     serving = saturated = None
@@ -602,7 +624,7 @@ def main():
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
                 "serving_saturated": saturated, "gridded": gridded, "configs": configs,
                 "gpu_launches": int(st_b["kernels_launched"]) * args.steps,
-                "gpu_launches_per_step": {"plane": 2, "hit": 1, "rank": 3, "transfer": 1},
+                "gpu_launches_per_step": {"plane": 2, "hit": 1, "rank": 3, "tau": 1, "iquv_rank": 3, "iquv": 1},
                 "autotuned_shape": tuning, "rhs_evals_per_step": st_b["rhs_evals"],
                 "steps_accepted": st_b["steps_accepted"], "steps_rejected": st_b["steps_rejected"]}
         print(json.dumps(line), flush=True)

@@ -264,6 +264,11 @@ typedef struct jsh_params {
  * that family's fused coefficient path alone (fewer registers, more
  * resident warps).  Results are bitwise the same; for comparison. */
 #define JSH_FLAG_GENERAL_KERNELS 0x10
+/* Mixed persistent schedule: record CUDA events on the launching stream
+ * around the tau kernel, the IQUV ranking kernels and the IQUV kernel, read
+ * back with jsh_last_kernel_ms (per-kernel device time for roofline
+ * figures).  Results are unchanged. */
+#define JSH_FLAG_KERNEL_TIMES 0x20
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,
@@ -552,6 +557,14 @@ int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model,
  * (TFLOP/s), each from a dependent-chain microbenchmark over every SM.
  * No reference counterpart (the reference has no device code). */
 int jsh_device_peaks(jsh_ctx* ctx, double* fp32_tflops, double* mufu_tops, double* fp64_tflops);
+
+/* Device times [ms] of the last request enqueued on the context with
+ * JSH_FLAG_KERNEL_TIMES on the mixed persistent schedule: the tau kernel,
+ * the IQUV ranking kernels and the IQUV kernel (the single-kernel form
+ * reports its one kernel as iquv_ms and 0 for the others).  Waits for the
+ * request's kernels.  JSH_ERR_NOT_FOUND when the last request did not ask
+ * for them.  No reference counterpart. */
+int jsh_last_kernel_ms(jsh_ctx* ctx, double* tau_ms, double* iquv_rank_ms, double* iquv_ms);
 
 /* Host-to-device bytes that one jsh_observation_run or
  * jsh_observation_run_device call copies: the compiled request record, the

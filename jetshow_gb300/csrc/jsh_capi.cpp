@@ -294,6 +294,8 @@ extern "C" void jsh_ctx_destroy(jsh_ctx* c) {
   if (c->ev_start) cudaEventDestroy(c->ev_start);
   if (c->ev_stop) cudaEventDestroy(c->ev_stop);
   if (c->ws_ready) cudaEventDestroy(c->ws_ready);
+  for (auto& e : c->kmarks)
+    if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -363,6 +365,15 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
   JSH_CUDA_TRY(jsh_launch_hit(d_req, 1, npix, stream));
   JshLaunchShape shape = jsh_effective_shape(ctx, params);
   shape.fused = (req.mix.helical_log && !(params->flags & JSH_FLAG_GENERAL_KERNELS)) ? 1 : 0;
+  shape.marks = nullptr;
+  ctx->kmarks_set = false;
+  if ((params->flags & JSH_FLAG_KERNEL_TIMES) && params->precision == JSH_PREC_MIXED &&
+      params->schedule == JSH_SCHED_PERSISTENT) {
+    for (auto& e : ctx->kmarks)
+      if (!e) JSH_CUDA_TRY(cudaEventCreate(&e));
+    shape.marks = ctx->kmarks;
+    ctx->kmarks_set = true;
+  }
   JSH_CUDA_TRY(jsh_launch_transfer(d_req, 1, params->precision, params->schedule, params->output == JSH_OUT_FULL,
                                    npix * (uint64_t)n_nu, npix, shape, (unsigned int*)(base + L.off_queue),
                                    ctx->num_sms, stream));
@@ -614,4 +625,25 @@ extern "C" uint64_t jsh_request_h2d_bytes(int32_t n_nu, int32_t precision) {
   uint64_t b = sizeof(JshRequest) + sizeof(double) * (uint64_t)n_nu;
   if (precision == JSH_PREC_MIXED) b += sizeof(JshFreqConst) * (uint64_t)n_nu;
   return b;
+}
+
+extern "C" int jsh_last_kernel_ms(jsh_ctx* ctx, double* tau_ms, double* iquv_rank_ms, double* iquv_ms) {
+  if (!ctx) {
+    jsh_set_error("null context");
+    return JSH_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!ctx->kmarks_set) {
+    jsh_set_error("the last request was not enqueued with JSH_FLAG_KERNEL_TIMES on the mixed persistent schedule");
+    return JSH_ERR_NOT_FOUND;
+  }
+  JSH_CUDA_TRY(cudaEventSynchronize(ctx->kmarks[3]));
+  float a = 0.f, b = 0.f, c = 0.f;
+  JSH_CUDA_TRY(cudaEventElapsedTime(&a, ctx->kmarks[0], ctx->kmarks[1]));
+  JSH_CUDA_TRY(cudaEventElapsedTime(&b, ctx->kmarks[1], ctx->kmarks[2]));
+  JSH_CUDA_TRY(cudaEventElapsedTime(&c, ctx->kmarks[2], ctx->kmarks[3]));
+  if (tau_ms) *tau_ms = a;
+  if (iquv_rank_ms) *iquv_rank_ms = b;
+  if (iquv_ms) *iquv_ms = c;
+  return JSH_OK;
 }

@@ -57,6 +57,8 @@ struct jsh_ctx {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ws_ready = nullptr;
+  cudaEvent_t kmarks[4] = {nullptr, nullptr, nullptr, nullptr};  // JSH_FLAG_KERNEL_TIMES
+  bool kmarks_set = false;
   std::mutex mu;
   uint64_t budget = 0;
   std::atomic<uint64_t> used{0};

@@ -17,6 +17,10 @@ struct JshLaunchShape {
   int single;            // mixed persistent schedule: tau and IQUV passes in one kernel (else split)
   int fused;             // split form: every request of the batch is of the fused benchmark
                          // family (mix.helical_log): launch the kernels built for it alone
+  // mixed persistent schedule, optional: four events recorded on the stream
+  // before the tau kernel, after it, after the IQUV ranking and after the
+  // IQUV kernel (the single-kernel form records the first three together)
+  cudaEvent_t* marks;
 };
 
 // Ray generation: along sizes and centres (sequential recurrence of

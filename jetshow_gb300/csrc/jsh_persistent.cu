@@ -1198,15 +1198,21 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
     unsigned bl_t = (unsigned)(num_sms * per_sm_t);
     if ((uint64_t)bl_t * bt > need) bl_t = (unsigned)((need + bt - 1) / bt);
     if (bl_t == 0) bl_t = 1;
+    if (shape.marks) cudaEventRecord(shape.marks[0], stream);
     if (shape.fused)
       transfer_tau_kernel<false><<<bl_t, bt, stage_smem<false>(bt), stream>>>(d_reqs, n_req, q, rf);
     else
       transfer_tau_kernel<true><<<bl_t, bt, stage_smem<false>(bt), stream>>>(d_reqs, n_req, q, rf);
+    if (shape.marks) cudaEventRecord(shape.marks[1], stream);
     const dim3 gi((unsigned)num_sms, (unsigned)n_req);
     iquv_hist_kernel<<<gi, 256, 0, stream>>>(d_reqs);
     iquv_prefix_kernel<<<n_req, 32, 0, stream>>>(d_reqs);
     iquv_scatter_kernel<<<gi, 256, 0, stream>>>(d_reqs);
+  } else if (shape.marks) {
+    cudaEventRecord(shape.marks[0], stream);
+    cudaEventRecord(shape.marks[1], stream);
   }
+  if (shape.marks) cudaEventRecord(shape.marks[2], stream);
   int bs = shape.block_size;
   if (bs > (shape.compact ? 128 : 256)) bs = shape.compact ? 128 : 256;
   int per_sm = shape.ctas_per_sm > 0 ? shape.ctas_per_sm : occupancy_mixed(split, full, bs, shape.compact);
@@ -1240,6 +1246,7 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
     if (full) transfer_persistent_mixed_kernel<true, false><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q, rf);
     else transfer_persistent_mixed_kernel<false, false><<<blocks, bs, smem, stream>>>(d_reqs, n_req, q, rf);
   }
+  if (shape.marks) cudaEventRecord(shape.marks[3], stream);
   return cudaGetLastError();
 }
 

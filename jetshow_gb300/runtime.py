@@ -102,6 +102,13 @@ class Context:
         return {"block_size": t.block_size, "ctas_per_sm": t.ctas_per_sm, "refill_threshold": t.refill_threshold,
                 "compact": t.compact, "ms": t.ms}
 
+    def last_kernel_ms(self):
+        """Device times [ms] of the last request's tau kernel, IQUV ranking and
+        IQUV kernel (it must have been enqueued with FLAG_KERNEL_TIMES)."""
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        check(self.lib, self.lib.jsh_last_kernel_ms(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return {"tau_ms": a.value, "iquv_rank_ms": b.value, "iquv_ms": c.value}
+
     def last_stats(self):
         st = A.Stats()
         check(self.lib, self.lib.jsh_last_stats(self.handle, C.byref(st)))

@@ -144,3 +144,24 @@ def test_split_kernels_match_single_kernel(ctx, flags, output):
     assert (sg["steps_accepted"], sg["steps_rejected"]) == (sr["steps_accepted"], sr["steps_rejected"])
     if flags != A.FLAG_SINGLE_KERNEL:
         assert sg["kernels_launched"] == 11
+
+
+def test_kernel_times(ctx):
+    """JSH_FLAG_KERNEL_TIMES: the tau, IQUV-ranking and IQUV kernel times of
+    the split form are positive and within the render's device time; the
+    single-kernel form reports its one kernel; images are unchanged."""
+    jet, plane, nu, _ = W.conical_c1(scale=8)
+    kw = dict(W.ACCURATE_KW)
+    a, sa = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent",
+                                                                   flags=A.FLAG_KERNEL_TIMES, **kw))
+    k = ctx.last_kernel_ms()
+    assert k["tau_ms"] > 0 and k["iquv_ms"] > 0 and k["iquv_rank_ms"] >= 0
+    assert k["tau_ms"] + k["iquv_rank_ms"] + k["iquv_ms"] <= sa["device_ms"] * 1.001
+    b, _ = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent", **kw))
+    assert np.array_equal(a["I"], b["I"]) and np.array_equal(a["tau"], b["tau"])
+    with pytest.raises(Exception):
+        ctx.last_kernel_ms()  # the last request did not ask for them
+    ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent",
+                                                          flags=A.FLAG_KERNEL_TIMES | A.FLAG_SINGLE_KERNEL, **kw))
+    k = ctx.last_kernel_ms()
+    assert k["tau_ms"] == 0 and k["iquv_ms"] > 0
