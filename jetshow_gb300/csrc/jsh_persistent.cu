@@ -613,7 +613,14 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
 #pragma unroll 1
     for (int s = 1; s < 7; ++s) {
       float acc[NK];
-      combine<NK>(s, K, acc);
+      // dtau/dt = k_I does not depend on the state: a tau step needs only
+      // the last combination (its increment), not the stage states
+      if (!tau || s == 6) {
+        combine<NK>(s, K, acc);
+      } else {
+#pragma unroll
+        for (int c = 0; c < NK; ++c) acc[c] = 0.f;
+      }
       float y[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) y[c] = (c < NX) ? fmaf(h, acc[c < NK ? c : 0], L.x[c]) : 0.f;
