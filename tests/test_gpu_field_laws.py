@@ -10,7 +10,8 @@ one B, N or V law swapped in and the others at the benchmark model's
   sequence sensitive to last-bit differences, and tight tolerances keep the
   two implementations within the contract gates of each other.
 * Mixed precision (FP32 stages) against the converged oracle (rtol 1e-10)
-  at the accuracy-qualified tolerances.
+  at the accuracy-qualified tolerances; the laws whose field jumps or flips
+  sign along a ray with the tau pass's steps limited (LAW_MIXED_KW).
 Reference quirks reproduced: ShearedCentralVField evaluates acos(z + o_z/r)
 with z in cm (src/VField.cpp:83), a NaN for every point of a real jet: the
 oracle and both device paths flag every hit item JSH_ST_NAN.
@@ -29,6 +30,15 @@ pytestmark = pytest.mark.gpu
 
 PC = J.pc
 TIGHT_KW = dict(W.ACCURATE_KW, tau_rtol=1e-11, rtol=1e-10)
+# Laws whose field jumps or flips direction along a ray (the composite
+# exponent at z0, the atan(y/x) sign flip at x = 0): at ACCURATE_KW a few
+# rays of the mixed path land at 1.6e-5 .. 3.4e-5 in tau (I 1.1e-4 for the
+# composite scalar field) against the converged oracle, because a step that
+# straddles the feature is accepted on an FP32 error estimate.  Limiting the
+# tau pass's steps to 0.01 pc and running IQUV at rtol 1e-7 brings every one
+# within the gates (measured: tau <= 4.7e-6, I <= 1.5e-5) for 3-4x the work.
+LAW_MIXED_KW = dict(W.ACCURATE_KW, rtol=1e-7, dt_max=0.01 * PC)
+STEP_LIMITED = {"CompositeRandomScalarBFieldZ", "ToroidalBField", "ToroidalBField_lab", "HelicalConicalBField_atan"}
 
 B_LAWS = {
     "RandomScalarBField": lambda: J.RandomScalarBField(0.1, 1.0),
@@ -106,7 +116,7 @@ def test_field_law_fp64_vs_oracle(ctx, oracle, kind, name):
 @pytest.mark.parametrize("kind,name", CASES)
 def test_field_law_mixed_vs_converged(ctx, oracle, kind, name):
     jet, plane, nu = case_model(kind, name)
-    g, st = ctx.render(jet.desc(), plane.desc(), nu,
-                       J.make_params(precision="mixed", schedule="persistent", **W.ACCURATE_KW))
+    kw = LAW_MIXED_KW if name in STEP_LIMITED else W.ACCURATE_KW
+    g, st = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent", **kw))
     r = oracle.render(jet.desc(), plane.desc(), nu, J.make_params(**W.CONVERGED_KW))
     check_case(flat(g), r, {})
