@@ -269,6 +269,16 @@ typedef struct jsh_params {
  * back with jsh_last_kernel_ms (per-kernel device time for roofline
  * figures).  Results are unchanged. */
 #define JSH_FLAG_KERNEL_TIMES 0x20
+/* Split form: run the passes as one serial chain.  By default a request of
+ * at least 65536 work items overlaps them: the rays estimated deepest (the
+ * optical depth of the ranking >= 8 at the first frequency) run their tau
+ * pass first, then their IQUV pass, which holds the render's longest items,
+ * at high priority beside the other rays' tau and IQUV passes (a second
+ * stream of the context, joined before the call's work ends on the caller's
+ * stream).  With overlapped passes the times of JSH_FLAG_KERNEL_TIMES are
+ * those of the phases: both tau kernels, the other rays' IQUV ranking, and
+ * the rest.  Results are bitwise the same. */
+#define JSH_FLAG_SERIAL_PASSES 0x40
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,
@@ -561,7 +571,8 @@ int jsh_device_peaks(jsh_ctx* ctx, double* fp32_tflops, double* mufu_tops, doubl
 /* Device times [ms] of the last request enqueued on the context with
  * JSH_FLAG_KERNEL_TIMES on the mixed persistent schedule: the tau kernel,
  * the IQUV ranking kernels and the IQUV kernel (the single-kernel form
- * reports its one kernel as iquv_ms and 0 for the others).  Waits for the
+ * reports its one kernel as iquv_ms and 0 for the others; overlapped passes
+ * report phases, see JSH_FLAG_SERIAL_PASSES).  Waits for the
  * request's kernels.  JSH_ERR_NOT_FOUND when the last request did not ask
  * for them.  No reference counterpart. */
 int jsh_last_kernel_ms(jsh_ctx* ctx, double* tau_ms, double* iquv_rank_ms, double* iquv_ms);
@@ -572,6 +583,15 @@ int jsh_last_kernel_ms(jsh_ctx* ctx, double* tau_ms, double* iquv_rank_ms, doubl
  * constants.  The descriptors themselves are read on the host.  No device
  * work; no reference counterpart. */
 uint64_t jsh_request_h2d_bytes(int32_t n_nu, int32_t precision);
+
+/* The panel rule of the mixed-precision tau pass for the smooth benchmark
+ * family (helical conical B and BK n in the plasma frame, flat flow): the
+ * 7/15-point Gauss-Kronrod rule on [-1, 1], 15 nodes ascending (x), Kronrod
+ * weights (wk) and Gauss weights (wg, zero at the Kronrod-only nodes), in
+ * FP64; the device holds them in FP32 on [0, 1].  For tests of the rule;
+ * no device work, no reference counterpart (the reference integrates tau
+ * with Dormand-Prince steps, src/Observation.cpp:150-211). */
+void jsh_tau_panel_rule(double* x, double* wk, double* wg);
 
 #ifdef __cplusplus
 }

@@ -35,6 +35,7 @@ FLAG_COMPACT_REGS = 0x4
 FLAG_SINGLE_KERNEL = 0x8
 FLAG_GENERAL_KERNELS = 0x10
 FLAG_KERNEL_TIMES = 0x20
+FLAG_SERIAL_PASSES = 0x40
 ST_ERRORS = ST_STEP_LIMIT | ST_FAIL_LIMIT | ST_BISECT_LIMIT | ST_NAN | ST_DT_UNDERFLOW
 
 GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE, GEO_SIMULATION = 1, 2, 3, 4, 5
@@ -299,6 +300,7 @@ SIGNATURES = [
     ("jsh_device_peaks", C.c_int, [C.c_void_p, _D, _D, _D]),
     ("jsh_request_h2d_bytes", C.c_uint64, [C.c_int32, C.c_int32]),
     ("jsh_last_kernel_ms", C.c_int, [C.c_void_p, _D, _D, _D]),
+    ("jsh_tau_panel_rule", None, [_D, _D, _D]),
     ("jsh_autotune", C.c_int,
      [C.c_void_p, _P(ModelDesc), _P(PlaneDesc), _D, C.c_int32, _P(Params), _P(Tuning)]),
 ]

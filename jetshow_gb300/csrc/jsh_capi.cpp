@@ -11,6 +11,7 @@
 #include <cmath>
 #include <vector>
 
+#include "jsh_quadrature.h"
 #include "jsh_context.h"
 
 namespace {
@@ -66,13 +67,13 @@ void jsh_request_layout(uint64_t npix, uint64_t n_along, uint64_t n_across, int3
   L->off_nhit = o;
   o = align_up(o + sizeof(uint32_t));
   L->off_queue = o;
-  o = align_up(o + sizeof(uint32_t));
+  o = align_up(o + 4 * sizeof(unsigned long long));
   L->off_buckets = o;
-  o = align_up(o + sizeof(uint32_t) * JSH_RANK_BUCKETS * 2);
+  o = align_up(o + sizeof(uint32_t) * JSH_RANK_WORDS);
   L->off_iq_count = o;
-  o = align_up(o + sizeof(uint32_t));
+  o = align_up(o + 2 * sizeof(uint32_t));
   L->off_iq_buckets = o;
-  o = align_up(o + sizeof(uint32_t) * JSH_RANK_BUCKETS * 2);
+  o = align_up(o + sizeof(uint32_t) * JSH_IQ_WORDS);
   L->off_nu = o;
   o = align_up(o + sizeof(double) * n_nu);
   L->off_fc = o;
@@ -128,9 +129,14 @@ void jsh_bind_request(JshRequest* req, char* base, const JshRequestLayout& L, bo
   }
 }
 
-int jsh_kernels_per_request(int precision, int schedule, bool single) {
-  if (precision == JSH_PREC_MIXED && schedule == JSH_SCHED_PERSISTENT) return single ? 7 : 11;
+int jsh_kernels_per_request(int precision, int schedule, bool single, bool overlap) {
+  if (precision == JSH_PREC_MIXED && schedule == JSH_SCHED_PERSISTENT) return single ? 7 : (overlap ? 15 : 11);
   return 4;
+}
+
+bool jsh_overlap_passes(const jsh_params* params, const JshLaunchShape& shape, uint64_t items) {
+  return params->precision == JSH_PREC_MIXED && params->schedule == JSH_SCHED_PERSISTENT && !shape.single &&
+         !(params->flags & JSH_FLAG_SERIAL_PASSES) && shape.overlap_key > 0 && items >= JSH_OVERLAP_MIN_ITEMS;
 }
 
 JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params) {
@@ -264,6 +270,9 @@ extern "C" int jsh_ctx_create(int device, uint64_t hbm_budget_bytes, jsh_ctx** o
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev_start) != cudaSuccess || cudaEventCreate(&c->ev_stop) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ws_ready, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->fork[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->fork[1], cudaEventDisableTiming) != cudaSuccess ||
       cudaMallocHost((void**)&c->h_req, sizeof(JshRequest)) != cudaSuccess ||
       cudaMallocHost((void**)&c->h_fc, 4096 * sizeof(JshFreqConst)) != cudaSuccess ||
       cudaMallocHost((void**)&c->h_counters, 8 * sizeof(unsigned long long)) != cudaSuccess) {
@@ -296,6 +305,9 @@ extern "C" void jsh_ctx_destroy(jsh_ctx* c) {
   if (c->ws_ready) cudaEventDestroy(c->ws_ready);
   for (auto& e : c->kmarks)
     if (e) cudaEventDestroy(e);
+  for (auto& e : c->fork)
+    if (e) cudaEventDestroy(e);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -366,6 +378,9 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
   JshLaunchShape shape = jsh_effective_shape(ctx, params);
   shape.fused = (req.mix.helical_log && !(params->flags & JSH_FLAG_GENERAL_KERNELS)) ? 1 : 0;
   shape.marks = nullptr;
+  const bool overlap = jsh_overlap_passes(params, shape, npix * (uint64_t)n_nu);
+  shape.side = overlap ? ctx->side : nullptr;
+  shape.fork = overlap ? ctx->fork : nullptr;
   ctx->kmarks_set = false;
   if ((params->flags & JSH_FLAG_KERNEL_TIMES) && params->precision == JSH_PREC_MIXED &&
       params->schedule == JSH_SCHED_PERSISTENT) {
@@ -373,6 +388,7 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
       if (!e) JSH_CUDA_TRY(cudaEventCreate(&e));
     shape.marks = ctx->kmarks;
     ctx->kmarks_set = true;
+    ctx->kmarks_single = shape.single != 0;
   }
   JSH_CUDA_TRY(jsh_launch_transfer(d_req, 1, params->precision, params->schedule, params->output == JSH_OUT_FULL,
                                    npix * (uint64_t)n_nu, npix, shape, (unsigned int*)(base + L.off_queue),
@@ -381,7 +397,8 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
   ctx->last_pending = true;
   // plane (2), hit, transfer; the persistent mixed schedule adds 3 ranking
   // kernels, and its split form the tau kernel and 3 IQUV ranking kernels
-  ctx->last_kernels = jsh_kernels_per_request(params->precision, params->schedule, shape.single != 0);
+  // (twice over when the passes overlap)
+  ctx->last_kernels = jsh_kernels_per_request(params->precision, params->schedule, shape.single != 0, overlap);
   ctx->last_counters_off = L.off_counters;
   ctx->last_nhit_off = L.off_nhit;
   ctx->last_npix = npix;
@@ -627,6 +644,14 @@ extern "C" uint64_t jsh_request_h2d_bytes(int32_t n_nu, int32_t precision) {
   return b;
 }
 
+extern "C" void jsh_tau_panel_rule(double* x, double* wk, double* wg) {
+  for (int i = 0; i < 15; ++i) {
+    if (x) x[i] = jsh_gk15_x[i];
+    if (wk) wk[i] = jsh_gk15_wk[i];
+    if (wg) wg[i] = jsh_gk15_wg[i];
+  }
+}
+
 extern "C" int jsh_last_kernel_ms(jsh_ctx* ctx, double* tau_ms, double* iquv_rank_ms, double* iquv_ms) {
   if (!ctx) {
     jsh_set_error("null context");
@@ -639,8 +664,10 @@ extern "C" int jsh_last_kernel_ms(jsh_ctx* ctx, double* tau_ms, double* iquv_ran
   }
   JSH_CUDA_TRY(cudaEventSynchronize(ctx->kmarks[3]));
   float a = 0.f, b = 0.f, c = 0.f;
-  JSH_CUDA_TRY(cudaEventElapsedTime(&a, ctx->kmarks[0], ctx->kmarks[1]));
-  JSH_CUDA_TRY(cudaEventElapsedTime(&b, ctx->kmarks[1], ctx->kmarks[2]));
+  if (!ctx->kmarks_single) {
+    JSH_CUDA_TRY(cudaEventElapsedTime(&a, ctx->kmarks[0], ctx->kmarks[1]));
+    JSH_CUDA_TRY(cudaEventElapsedTime(&b, ctx->kmarks[1], ctx->kmarks[2]));
+  }
   JSH_CUDA_TRY(cudaEventElapsedTime(&c, ctx->kmarks[2], ctx->kmarks[3]));
   if (tau_ms) *tau_ms = a;
   if (iquv_rank_ms) *iquv_rank_ms = b;

@@ -58,7 +58,11 @@ struct jsh_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ws_ready = nullptr;
   cudaEvent_t kmarks[4] = {nullptr, nullptr, nullptr, nullptr};  // JSH_FLAG_KERNEL_TIMES
-  bool kmarks_set = false;
+  bool kmarks_set = false, kmarks_single = false;
+  // overlapped passes of the split form: the second stream and the fork /
+  // join events (created with the context)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork[2] = {nullptr, nullptr};
   std::mutex mu;
   uint64_t budget = 0;
   std::atomic<uint64_t> used{0};
@@ -71,7 +75,7 @@ struct jsh_ctx {
   JshHullSlot hulls[JSH_MAX_HULLS];
   JshCellSlot cells[JSH_MAX_CELL_SETS];
   bool tuned = false;
-  JshLaunchShape shape{128, 0, 8, 0};
+  JshLaunchShape shape{128, 0, 8, 0, 0, 0, nullptr, JSH_OVERLAP_KEY};
   jsh_stats last{};
   bool last_pending = false;
   size_t last_counters_off = 0, last_nhit_off = 0;
@@ -97,7 +101,11 @@ JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params)
 // ranges the launchers accept; needs no context.
 JshLaunchShape jsh_params_shape(JshLaunchShape s, const jsh_params* params);
 // Kernels one request launches (plane, hit, ranking, transfer).
-int jsh_kernels_per_request(int precision, int schedule, bool single);
+int jsh_kernels_per_request(int precision, int schedule, bool single, bool overlap = false);
+// Whether a request of `items` work items runs the split form's passes
+// overlapped (large requests on the mixed persistent schedule, unless
+// JSH_FLAG_SERIAL_PASSES or the single-kernel form).
+bool jsh_overlap_passes(const jsh_params* params, const JshLaunchShape& shape, uint64_t items);
 // Grow the context workspace to `need` bytes (waits for its previous user).
 int ensure_workspace(jsh_ctx* ctx, size_t need);
 // Enqueue one request on `stream` in the context workspace; dev_out NULL

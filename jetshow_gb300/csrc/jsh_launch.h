@@ -8,6 +8,11 @@
 #include "jsh_request.h"
 
 #define JSH_MAX_BATCH 64
+// Default deep-prefix bucket of overlapped passes (estimated optical depth
+// of a ray at the request's first frequency >= 8), and the smallest request
+// (work items) that overlaps them.
+#define JSH_OVERLAP_KEY 43
+#define JSH_OVERLAP_MIN_ITEMS 65536
 
 struct JshLaunchShape {
   int block_size;        // threads per CTA of the transfer kernel
@@ -19,8 +24,19 @@ struct JshLaunchShape {
                          // family (mix.helical_log): launch the kernels built for it alone
   // mixed persistent schedule, optional: four events recorded on the stream
   // before the tau kernel, after it, after the IQUV ranking and after the
-  // IQUV kernel (the single-kernel form records the first three together)
+  // IQUV kernel (the single-kernel form records only the last two;
+  // with overlapped passes: before the deep prefix's tau kernel, after the
+  // other rays' tau kernel and IQUV ranking, and after both IQUV kernels)
   cudaEvent_t* marks;
+  // split form, optional: overlapped passes.  Rays whose rank bucket is at
+  // least overlap_key (estimated optical depth >= 2^(overlap_key - 40)) form
+  // the deep prefix: its tau pass runs first and its IQUV pass, which holds
+  // the render's longest items, runs on `stream` at high priority while the
+  // other rays' tau and IQUV passes run on `side` (fork[0] / fork[1]: events
+  // of the fork and the join).  0 or no side stream: one serial chain.
+  int overlap_key;
+  cudaStream_t side;
+  cudaEvent_t* fork;
 };
 
 // Ray generation: along sizes and centres (sequential recurrence of

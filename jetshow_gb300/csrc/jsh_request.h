@@ -16,6 +16,14 @@ struct JshHit {           // one intersecting pixel (Intersection list)
 
 // Cost buckets of the heaviest-first ranking (factors of 2 in optical depth).
 #define JSH_RANK_BUCKETS 64
+// Words of a request's ranking state: bucket counts, bucket cursors, then
+// the number of ranked rays in the deep prefix (the rays whose passes run
+// ahead of the others when the split form overlaps them; all rays when not).
+#define JSH_RANK_DEEP (2 * JSH_RANK_BUCKETS)
+#define JSH_RANK_WORDS (2 * JSH_RANK_BUCKETS + 32)
+// Words of a request's IQUV ranking state: counts and cursors of the deep
+// prefix's emitted items, then those of the other rays' items.
+#define JSH_IQ_WORDS (4 * JSH_RANK_BUCKETS)
 
 // Persistent mixed schedule, split form: one work item whose tau pass has
 // finished and whose I/IQUV pass is still to run, as the tau kernel hands it
@@ -92,16 +100,18 @@ struct JshRequest {
   JshParamsDev P;
   JshHit* hits;           // device [npix] (first n_hit valid)
   // persistent mixed schedule: hit rays ranked by estimated cost, heaviest
-  // first (order[rank] = hit index), their cost buckets and the bucket
-  // counts / cursors [2][JSH_RANK_BUCKETS] (zeroed with the counters)
+  // first (order[rank] = hit index), their cost buckets and the ranking
+  // state [JSH_RANK_WORDS] (zeroed with the counters)
   uint32_t* order;
   uint8_t* key;
   uint32_t* buckets;
   uint32_t* n_hit;        // device counter written by the hit kernel
   // persistent mixed schedule, split form: items handed from the tau kernel
   // to the IQUV kernel [npix * n_nu], their heaviest-first order, their
-  // count and the cost-bucket counts / cursors [2][JSH_RANK_BUCKETS] (count
-  // and buckets zeroed with the counters)
+  // counts [2] and the IQUV ranking state [JSH_IQ_WORDS] (counts and state
+  // zeroed with the counters).  The deep prefix's items fill the array from
+  // 0, the other rays' items from n_deep * n_nu (n_deep =
+  // buckets[JSH_RANK_DEEP]); iq_order holds absolute item indices.
   JshIquvItem* iq_items;
   uint32_t* iq_order;
   uint32_t* iq_count;

@@ -159,15 +159,15 @@ struct jsh_server {
 namespace {
 
 // Counters region of slot s: [JSH_MAX_BATCH][8] u64 counters, n_hit[JSH_MAX_BATCH],
-// [JSH_MAX_BATCH][2][JSH_RANK_BUCKETS] rank buckets, the IQUV item counts
-// [JSH_MAX_BATCH] and their [JSH_MAX_BATCH][2][JSH_RANK_BUCKETS] cost
-// buckets, then the queue counters.
+// [JSH_MAX_BATCH][JSH_RANK_WORDS] ranking state, the IQUV item counts
+// [JSH_MAX_BATCH][2] and their [JSH_MAX_BATCH][JSH_IQ_WORDS] ranking state,
+// then the queue counters (256 bytes).
 size_t nhit_off() { return align_up(sizeof(unsigned long long) * 8 * JSH_MAX_BATCH); }
 size_t buckets_off() { return nhit_off() + align_up(sizeof(uint32_t) * JSH_MAX_BATCH); }
-size_t iq_count_off() { return buckets_off() + align_up(sizeof(uint32_t) * 2 * JSH_RANK_BUCKETS * JSH_MAX_BATCH); }
-size_t iq_buckets_off() { return iq_count_off() + align_up(sizeof(uint32_t) * JSH_MAX_BATCH); }
+size_t iq_count_off() { return buckets_off() + align_up(sizeof(uint32_t) * JSH_RANK_WORDS * JSH_MAX_BATCH); }
+size_t iq_buckets_off() { return iq_count_off() + align_up(sizeof(uint32_t) * 2 * JSH_MAX_BATCH); }
 size_t counters_region_bytes() {
-  return iq_buckets_off() + align_up(sizeof(uint32_t) * 2 * JSH_RANK_BUCKETS * JSH_MAX_BATCH) + 256;
+  return iq_buckets_off() + align_up(sizeof(uint32_t) * JSH_IQ_WORDS * JSH_MAX_BATCH) + 256;
 }
 
 // Pointers of record i into the slot's counters region.
@@ -175,9 +175,9 @@ void bind_counters(JshRequest& r, char* ctl, size_t counters_off, int i) {
   char* c = ctl + counters_off;
   r.counters = (unsigned long long*)c + 8 * i;
   r.n_hit = (uint32_t*)(c + nhit_off()) + i;
-  r.buckets = (uint32_t*)(c + buckets_off()) + 2 * JSH_RANK_BUCKETS * i;
-  r.iq_count = (uint32_t*)(c + iq_count_off()) + i;
-  r.iq_buckets = (uint32_t*)(c + iq_buckets_off()) + 2 * JSH_RANK_BUCKETS * i;
+  r.buckets = (uint32_t*)(c + buckets_off()) + JSH_RANK_WORDS * i;
+  r.iq_count = (uint32_t*)(c + iq_count_off()) + 2 * i;
+  r.iq_buckets = (uint32_t*)(c + iq_buckets_off()) + JSH_IQ_WORDS * i;
 }
 
 int prepare_request(jsh_server* S, Request* q) {

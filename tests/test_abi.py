@@ -70,3 +70,23 @@ def test_request_h2d_bytes(lib):
     assert lib.jsh_request_h2d_bytes(4, A.PREC_FP64) == b1 + 3 * 8
     assert lib.jsh_request_h2d_bytes(4, A.PREC_MIXED) == b1 + 3 * 8 + 4 * 56
     assert 1024 < b1 < 4096
+
+
+def test_tau_panel_rule_is_gauss_kronrod(lib):
+    """The tau pass's panel rule: the 15-point Kronrod rule integrates
+    monomials of degree <= 22 exactly on [-1, 1], its embedded 7-point Gauss
+    rule those of degree <= 13 and equals the Gauss-Legendre rule."""
+    import ctypes as C
+    x, wk, wg = (np.zeros(15) for _ in range(3))
+    p = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    lib.jsh_tau_panel_rule(p(x), p(wk), p(wg))
+    assert np.all(np.diff(x) > 0) and np.allclose(x, -x[::-1], rtol=0, atol=1e-16)
+    for k in range(23):
+        exact = (1 - (-1) ** (k + 1)) / (k + 1)
+        assert abs((wk * x ** k).sum() - exact) < 1e-14, k
+        if k < 14:
+            assert abs((wg * x ** k).sum() - exact) < 1e-14, k
+    assert abs((wk * x ** 24).sum() - 2 / 25) > 1e-10  # not exact beyond degree 22
+    gx, gw = np.polynomial.legendre.leggauss(7)
+    assert np.allclose(x[1::2], gx, rtol=0, atol=1e-15) and np.allclose(wg[1::2], gw, rtol=0, atol=1e-15)
+    assert np.all(wg[0::2] == 0)

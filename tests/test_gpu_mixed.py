@@ -146,6 +146,45 @@ def test_split_kernels_match_single_kernel(ctx, flags, output):
         assert sg["kernels_launched"] == 11
 
 
+@pytest.mark.parametrize("output", ["full", "I"])
+@pytest.mark.parametrize("flags", [0, A.FLAG_GENERAL_KERNELS, A.FLAG_COMPACT_REGS, A.FLAG_IQUV_FROM_TAU_MAX])
+def test_overlapped_passes_match_serial(ctx, flags, output):
+    """Requests of >= 65536 work items overlap the split form's passes (the
+    deep rays' IQUV pass beside the other rays' tau and IQUV passes on a
+    second stream): every plane and counter bitwise those of the serial
+    chain (JSH_FLAG_SERIAL_PASSES), with each build of the kernels."""
+    jet, plane, nu, _ = W.conical_c1(scale=2)  # 206 368 work items
+    kw = dict(W.ACCURATE_KW, output=output)
+    ser, ss = ctx.render(jet.desc(), plane.desc(), nu,
+                         J.make_params(precision="mixed", schedule="persistent",
+                                       flags=flags | A.FLAG_SERIAL_PASSES | A.FLAG_COST_MAP, **kw))
+    ovl, so = ctx.render(jet.desc(), plane.desc(), nu,
+                         J.make_params(precision="mixed", schedule="persistent", flags=flags | A.FLAG_COST_MAP,
+                                       **kw))
+    for k in ("tau", "l", "I", "Q", "U", "V", "status"):
+        assert np.array_equal(ovl[k], ser[k]), k
+    for k in ("rhs_evals", "steps_accepted", "steps_rejected", "status_or"):
+        assert so[k] == ss[k], k
+    assert ss["kernels_launched"] == 11 and so["kernels_launched"] == 15
+
+
+@pytest.mark.parametrize("nu_factor", [0.25, 8.0])
+def test_overlapped_passes_deep_prefix_all_or_none(ctx, nu_factor):
+    """The deep prefix of overlapped passes at its extremes: at a quarter of
+    the frequencies most rays are deep (the other rays' chain is short), at
+    8x none is (the deep chain is empty); images bitwise those of the serial
+    chain."""
+    jet, plane, nu, _ = W.conical_c1(scale=2)
+    nu = np.asarray(nu) * nu_factor
+    kw = dict(W.ACCURATE_KW)
+    ser, ss = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent",
+                                                                     flags=A.FLAG_SERIAL_PASSES, **kw))
+    ovl, so = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent", **kw))
+    for k in ("tau", "I", "Q", "U", "V", "status"):
+        assert np.array_equal(ovl[k], ser[k]), k
+    assert so["rhs_evals"] == ss["rhs_evals"]
+
+
 def test_kernel_times(ctx):
     """JSH_FLAG_KERNEL_TIMES: the tau, IQUV-ranking and IQUV kernel times of
     the split form are positive and within the render's device time; the
@@ -165,3 +204,11 @@ def test_kernel_times(ctx):
                                                           flags=A.FLAG_KERNEL_TIMES | A.FLAG_SINGLE_KERNEL, **kw))
     k = ctx.last_kernel_ms()
     assert k["tau_ms"] == 0 and k["iquv_ms"] > 0
+    # overlapped passes (a larger request): phase times, within the render
+    jet, plane, nu, _ = W.conical_c1(scale=2)
+    _, sc = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent",
+                                                                   flags=A.FLAG_KERNEL_TIMES, **kw))
+    k = ctx.last_kernel_ms()
+    assert sc["kernels_launched"] == 15
+    assert k["tau_ms"] > 0 and k["iquv_ms"] > 0 and k["iquv_rank_ms"] >= 0
+    assert k["tau_ms"] + k["iquv_rank_ms"] + k["iquv_ms"] <= sc["device_ms"] * 1.001
