@@ -269,16 +269,19 @@ typedef struct jsh_params {
  * back with jsh_last_kernel_ms (per-kernel device time for roofline
  * figures).  Results are unchanged. */
 #define JSH_FLAG_KERNEL_TIMES 0x20
-/* Split form: run the passes as one serial chain.  By default a request of
- * at least 65536 work items overlaps them: the rays estimated deepest (the
- * optical depth of the ranking >= 8 at the first frequency) run their tau
- * pass first, then their IQUV pass, which holds the render's longest items,
- * at high priority beside the other rays' tau and IQUV passes (a second
- * stream of the context, joined before the call's work ends on the caller's
- * stream).  With overlapped passes the times of JSH_FLAG_KERNEL_TIMES are
- * those of the phases: both tau kernels, the other rays' IQUV ranking, and
- * the rest.  Results are bitwise the same. */
+/* Split form, requests of at least 65536 work items: overlap the passes.
+ * The rays estimated deepest (the optical depth of the ranking >= 8 at the
+ * first frequency) run their tau pass first, then their IQUV pass, which
+ * holds the render's longest items, at high priority beside the other rays'
+ * tau and IQUV passes (a second stream of the context, joined before the
+ * call's work ends on the caller's stream).  It pays when those items set
+ * the render's length; jsh_autotune tries it and keeps it for the context
+ * when faster (JSH_FLAG_SERIAL_PASSES then runs one serial chain).  With
+ * overlapped passes the times of JSH_FLAG_KERNEL_TIMES are those of the
+ * phases: both tau kernels, the other rays' IQUV ranking, and the rest.
+ * Results are bitwise the same either way. */
 #define JSH_FLAG_SERIAL_PASSES 0x40
+#define JSH_FLAG_OVERLAP_PASSES 0x80
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,
@@ -549,13 +552,15 @@ typedef struct jsh_tuning {
   int32_t ctas_per_sm;
   int32_t refill_threshold;
   int32_t compact;      /* 1: the register-capped build (JSH_FLAG_COMPACT_REGS) */
+  int32_t overlap;      /* 1: overlapped passes (JSH_FLAG_OVERLAP_PASSES) */
   double ms;            /* best measured time */
 } jsh_tuning;
 
 /* Time the persistent schedule over a grid of kernel builds (default and
- * register-capped), block sizes, CTAs per SM and refill thresholds on this
- * request and store the fastest in the context; later requests with
- * block_size == 0 use it. */
+ * register-capped), block sizes, CTAs per SM, refill thresholds and serial
+ * or overlapped passes on this request and store the fastest in the
+ * context; later requests with block_size == 0 use it (the overlap choice
+ * holds unless a request's flags force one). */
 int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model,
                  const jsh_plane_desc* plane, const double* nu_hz,
                  int32_t n_nu, const jsh_params* params, jsh_tuning* best);

@@ -36,6 +36,7 @@ FLAG_SINGLE_KERNEL = 0x8
 FLAG_GENERAL_KERNELS = 0x10
 FLAG_KERNEL_TIMES = 0x20
 FLAG_SERIAL_PASSES = 0x40
+FLAG_OVERLAP_PASSES = 0x80
 ST_ERRORS = ST_STEP_LIMIT | ST_FAIL_LIMIT | ST_BISECT_LIMIT | ST_NAN | ST_DT_UNDERFLOW
 
 GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE, GEO_SIMULATION = 1, 2, 3, 4, 5
@@ -235,6 +236,7 @@ class Tuning(C.Structure):
         ("ctas_per_sm", C.c_int32),
         ("refill_threshold", C.c_int32),
         ("compact", C.c_int32),
+        ("overlap", C.c_int32),
         ("ms", C.c_double),
     ]
 

@@ -8,8 +8,10 @@
 // queue).  The search times the caller's request under each shape with CUDA
 // events on the context stream: first a sweep over (build, block size, CTAs
 // per SM) at the current refill threshold, then a sweep of the refill
-// threshold at the best triple.  The fastest shape becomes the context default, used by
-// every later request whose params leave the knobs at 0.
+// threshold at the best triple, then serial against overlapped passes of
+// the split form (the deep rays' IQUV pass beside the other rays' passes)
+// at the best shape.  The fastest shape becomes the context default, used
+// by every later request whose params leave the knobs at 0.
 //
 // No counterpart in the reference, which renders on the CPU with an OpenMP
 // loop over pixels (src/Observation.cpp:44-48).
@@ -62,6 +64,8 @@ extern "C" int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model, const jsh
   JSH_CUDA_TRY(cudaSetDevice(ctx->device));
   jsh_params p = *params;
   p.schedule = JSH_SCHED_PERSISTENT;
+  // the shape sweeps time serial chains; overlap is tried last
+  p.flags = (p.flags | JSH_FLAG_SERIAL_PASSES) & ~JSH_FLAG_OVERLAP_PASSES;
   Timer T;
   JSH_CUDA_TRY(cudaEventCreate(&T.a));
   JSH_CUDA_TRY(cudaEventCreate(&T.b));
@@ -109,14 +113,32 @@ extern "C" int jsh_autotune(jsh_ctx* ctx, const jsh_model_desc* model, const jsh
       b_rf = rf;
     }
   }
+  // serial or overlapped passes (split form of the mixed schedule, requests
+  // large enough to overlap); the sweeps above ran serial chains
+  bool b_ov = false;
+  jsh_params po = p;
+  po.flags = (po.flags & ~JSH_FLAG_SERIAL_PASSES) | JSH_FLAG_OVERLAP_PASSES;
+  JshLaunchShape probe = ctx->shape;
+  probe.overlap_key = 0;
+  uint64_t npix = (uint64_t)plane->n_across * (uint64_t)plane->n_along;
+  if (jsh_overlap_passes(&po, jsh_params_shape(probe, &po), npix * (uint64_t)n_nu)) {
+    st = time_shape(ctx, T, model, plane, nu_hz, n_nu, po, b_bs, b_sm, b_rf, b_cp, &ms);
+    if (st) return st;
+    if (ms < b_ms) {
+      b_ms = ms;
+      b_ov = true;
+    }
+  }
   ctx->shape.block_size = b_bs;
   ctx->shape.ctas_per_sm = b_sm;
   ctx->shape.refill_threshold = b_rf;
   ctx->shape.compact = b_cp ? 1 : 0;
+  ctx->shape.overlap_key = b_ov ? JSH_OVERLAP_KEY : 0;
   best->block_size = b_bs;
   best->ctas_per_sm = b_sm;
   best->refill_threshold = b_rf;
   best->compact = b_cp ? 1 : 0;
+  best->overlap = b_ov ? 1 : 0;
   best->ms = b_ms;
   return JSH_OK;
 }

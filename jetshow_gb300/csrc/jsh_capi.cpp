@@ -136,7 +136,8 @@ int jsh_kernels_per_request(int precision, int schedule, bool single, bool overl
 
 bool jsh_overlap_passes(const jsh_params* params, const JshLaunchShape& shape, uint64_t items) {
   return params->precision == JSH_PREC_MIXED && params->schedule == JSH_SCHED_PERSISTENT && !shape.single &&
-         !(params->flags & JSH_FLAG_SERIAL_PASSES) && shape.overlap_key > 0 && items >= JSH_OVERLAP_MIN_ITEMS;
+         !(params->flags & JSH_FLAG_SERIAL_PASSES) &&
+         ((params->flags & JSH_FLAG_OVERLAP_PASSES) || shape.overlap_key > 0) && items >= JSH_OVERLAP_MIN_ITEMS;
 }
 
 JshLaunchShape jsh_effective_shape(const jsh_ctx* ctx, const jsh_params* params) {
@@ -379,6 +380,7 @@ int enqueue_single(jsh_ctx* ctx, const jsh_model_desc* model, const jsh_plane_de
   shape.fused = (req.mix.helical_log && !(params->flags & JSH_FLAG_GENERAL_KERNELS)) ? 1 : 0;
   shape.marks = nullptr;
   const bool overlap = jsh_overlap_passes(params, shape, npix * (uint64_t)n_nu);
+  if (overlap && shape.overlap_key <= 0) shape.overlap_key = JSH_OVERLAP_KEY;
   shape.side = overlap ? ctx->side : nullptr;
   shape.fork = overlap ? ctx->fork : nullptr;
   ctx->kmarks_set = false;

@@ -75,7 +75,7 @@ struct jsh_ctx {
   JshHullSlot hulls[JSH_MAX_HULLS];
   JshCellSlot cells[JSH_MAX_CELL_SETS];
   bool tuned = false;
-  JshLaunchShape shape{128, 0, 8, 0, 0, 0, nullptr, JSH_OVERLAP_KEY};
+  JshLaunchShape shape{128, 0, 8, 0};
   jsh_stats last{};
   bool last_pending = false;
   size_t last_counters_off = 0, last_nhit_off = 0;
@@ -103,7 +103,8 @@ JshLaunchShape jsh_params_shape(JshLaunchShape s, const jsh_params* params);
 // Kernels one request launches (plane, hit, ranking, transfer).
 int jsh_kernels_per_request(int precision, int schedule, bool single, bool overlap = false);
 // Whether a request of `items` work items runs the split form's passes
-// overlapped (large requests on the mixed persistent schedule, unless
+// overlapped (JSH_FLAG_OVERLAP_PASSES, or a context shape tuned to overlap
+// them; large requests on the mixed persistent schedule only, never with
 // JSH_FLAG_SERIAL_PASSES or the single-kernel form).
 bool jsh_overlap_passes(const jsh_params* params, const JshLaunchShape& shape, uint64_t items);
 // Grow the context workspace to `need` bytes (waits for its previous user).

@@ -8,9 +8,9 @@
 #include "jsh_request.h"
 
 #define JSH_MAX_BATCH 64
-// Default deep-prefix bucket of overlapped passes (estimated optical depth
-// of a ray at the request's first frequency >= 8), and the smallest request
-// (work items) that overlaps them.
+// Deep-prefix bucket of overlapped passes (estimated optical depth of a ray
+// at the request's first frequency >= 8), and the smallest request (work
+// items) that overlaps them.
 #define JSH_OVERLAP_KEY 43
 #define JSH_OVERLAP_MIN_ITEMS 65536
 

@@ -100,7 +100,7 @@ class Context:
         check(self.lib, self.lib.jsh_autotune(self.handle, C.byref(model), C.byref(plane), A.dptr(nu), nu.size,
                                               C.byref(params), C.byref(t)))
         return {"block_size": t.block_size, "ctas_per_sm": t.ctas_per_sm, "refill_threshold": t.refill_threshold,
-                "compact": t.compact, "ms": t.ms}
+                "compact": t.compact, "overlap": t.overlap, "ms": t.ms}
 
     def last_kernel_ms(self):
         """Device times [ms] of the last request's tau kernel, IQUV ranking and

@@ -149,18 +149,18 @@ def test_split_kernels_match_single_kernel(ctx, flags, output):
 @pytest.mark.parametrize("output", ["full", "I"])
 @pytest.mark.parametrize("flags", [0, A.FLAG_GENERAL_KERNELS, A.FLAG_COMPACT_REGS, A.FLAG_IQUV_FROM_TAU_MAX])
 def test_overlapped_passes_match_serial(ctx, flags, output):
-    """Requests of >= 65536 work items overlap the split form's passes (the
-    deep rays' IQUV pass beside the other rays' tau and IQUV passes on a
-    second stream): every plane and counter bitwise those of the serial
-    chain (JSH_FLAG_SERIAL_PASSES), with each build of the kernels."""
+    """Overlapped passes of the split form (JSH_FLAG_OVERLAP_PASSES, requests
+    of >= 65536 work items: the deep rays' IQUV pass beside the other rays'
+    tau and IQUV passes on a second stream): every plane and counter bitwise
+    those of the serial chain, with each build of the kernels."""
     jet, plane, nu, _ = W.conical_c1(scale=2)  # 206 368 work items
     kw = dict(W.ACCURATE_KW, output=output)
     ser, ss = ctx.render(jet.desc(), plane.desc(), nu,
                          J.make_params(precision="mixed", schedule="persistent",
                                        flags=flags | A.FLAG_SERIAL_PASSES | A.FLAG_COST_MAP, **kw))
     ovl, so = ctx.render(jet.desc(), plane.desc(), nu,
-                         J.make_params(precision="mixed", schedule="persistent", flags=flags | A.FLAG_COST_MAP,
-                                       **kw))
+                         J.make_params(precision="mixed", schedule="persistent",
+                                       flags=flags | A.FLAG_OVERLAP_PASSES | A.FLAG_COST_MAP, **kw))
     for k in ("tau", "l", "I", "Q", "U", "V", "status"):
         assert np.array_equal(ovl[k], ser[k]), k
     for k in ("rhs_evals", "steps_accepted", "steps_rejected", "status_or"):
@@ -179,7 +179,8 @@ def test_overlapped_passes_deep_prefix_all_or_none(ctx, nu_factor):
     kw = dict(W.ACCURATE_KW)
     ser, ss = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent",
                                                                      flags=A.FLAG_SERIAL_PASSES, **kw))
-    ovl, so = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent", **kw))
+    ovl, so = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent",
+                                                                     flags=A.FLAG_OVERLAP_PASSES, **kw))
     for k in ("tau", "I", "Q", "U", "V", "status"):
         assert np.array_equal(ovl[k], ser[k]), k
     assert so["rhs_evals"] == ss["rhs_evals"]
@@ -207,7 +208,8 @@ def test_kernel_times(ctx):
     # overlapped passes (a larger request): phase times, within the render
     jet, plane, nu, _ = W.conical_c1(scale=2)
     _, sc = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent",
-                                                                   flags=A.FLAG_KERNEL_TIMES, **kw))
+                                                                   flags=A.FLAG_KERNEL_TIMES | A.FLAG_OVERLAP_PASSES,
+                                                                   **kw))
     k = ctx.last_kernel_ms()
     assert sc["kernels_launched"] == 15
     assert k["tau_ms"] > 0 and k["iquv_ms"] > 0 and k["iquv_rank_ms"] >= 0

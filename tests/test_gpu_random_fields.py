@@ -74,11 +74,13 @@ def test_cells_random_field_fp64_vs_oracle(ctx, oracle, cells):
 
 def test_cells_random_field_mixed_vs_converged(ctx, oracle, cells):
     # the field jumps across every face between cells (a few hundred faces
-    # along a ray): the tau pass's steps limited to 0.003 pc, three times
-    # finer than for the laws with one jump (test_gpu_field_laws.LAW_MIXED_KW;
-    # at 0.01 pc the worst tau is 1.2e-5 off)
+    # along a ray), where the Dormand-Prince tau pass converges slowly: at
+    # tau_rtol 5e-8 the worst tau is 1.2e-5 .. 1.6e-5 off the converged
+    # oracle with steps of at most 0.01 or 0.003 pc, in FP64 on the device
+    # as well (1.5e-5 .. 1.7e-5: the reference's algorithm at that
+    # tolerance); tau_rtol 1e-9 with 0.003 pc steps gives 1.2e-6
     jet, plane, nu = model(J.CellsRandomVectorBField(cells, J.HelicalConicalBField(0.1, 1.0, math.pi / 4, False), 0.5))
-    kw = dict(W.ACCURATE_KW, rtol=1e-7, dt_max=0.003 * PC)
+    kw = dict(W.ACCURATE_KW, rtol=1e-7, tau_rtol=1e-9, dt_max=0.003 * PC)
     g, st = ctx.render(jet.desc(), plane.desc(), nu, J.make_params(precision="mixed", schedule="persistent", **kw))
     r = oracle.render(jet.desc(), plane.desc(), nu, J.make_params(**W.CONVERGED_KW))
     compare_images(flat(g), r, full=True, tau_max=1e4)
