@@ -17,15 +17,22 @@ constexpr int kHitThreads = 256;
 // pyLogspace by repeated multiplication and the running partial sum are
 // sequential recurrences (include/logspace.h:9-33, src/Image.cpp:70-75): one
 // thread per request walks them so every value rounds as in the reference.
+// The plane's fields are read into registers first: the table stores could
+// alias the request record as far as the compiler knows, which made it
+// reload them on every iteration (~300 cycles per column).
 __global__ void plane_along_kernel(const JshRequest* __restrict__ reqs) {
   if (threadIdx.x != 0) return;
   const JshPlane& p = reqs[blockIdx.x].plane;
+  double* __restrict__ size = p.along_size;
+  double* __restrict__ center = p.along_center;
+  const uint64_t n = p.n_along;
+  const double base = p.real_base;
   double cur = p.real_start, acc = 0.0;
-  for (uint64_t j = 0; j < p.n_along; ++j) {
-    p.along_size[j] = cur;
+  for (uint64_t j = 0; j < n; ++j) {
+    size[j] = cur;
     acc = (j == 0) ? cur : ad(acc, cur);
-    p.along_center[j] = sb(acc, ml(0.5, cur));
-    cur = ml(cur, p.real_base);
+    center[j] = sb(acc, ml(0.5, cur));
+    cur = ml(cur, base);
   }
 }
 
@@ -36,12 +43,13 @@ __global__ void plane_across_kernel(const JshRequest* __restrict__ reqs) {
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.n_along) return;
   uint64_t nh = p.n_across / 2, na = p.n_along;
+  double* __restrict__ pos = p.across_pos;
   double s = ml(p.along_size[j], 1.0);
   double half = ml(0.5, s);
   double a = 0.0;
   for (uint64_t k = 0; k < nh; ++k) {
     a = (k == 0) ? s : ad(a, s);
-    p.across_pos[k * na + j] = sb(a, half);
+    pos[k * na + j] = sb(a, half);
   }
 }
 
