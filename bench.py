@@ -57,9 +57,11 @@ CENSUS_TAU_FP32_INSTR = 34
 CENSUS_TAU_MUFU = 5
 # DRAM bytes (read + write) per launch of the two transfer kernels of the
 # split form, from an ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum) of the 256x512 render scaled to the full render by
-# its hit rays; None until captured for this build
-TRAFFIC_BYTES_PER_LAUNCH = {"transfer_tau_kernel": None, "transfer_iquv_kernel": None}
+# dram__bytes_write.sum) of the 256x512 render (206 368 work items; tau
+# kernel 6 537 472 + 1 024 B, IQUV kernel 13 360 384 + 54 272 B) scaled to
+# the full render by its work items (826 336)
+TRAFFIC_BYTES_PER_LAUNCH = {"transfer_tau_kernel": round((6537472 + 1024) * 826336 / 206368),
+                            "transfer_iquv_kernel": round((13360384 + 54272) * 826336 / 206368)}
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of each transfer kernel on the "
                   "256x512 render, scaled by the hit rays")
 

@@ -17,9 +17,11 @@ constexpr int kHitThreads = 256;
 // pyLogspace by repeated multiplication and the running partial sum are
 // sequential recurrences (include/logspace.h:9-33, src/Image.cpp:70-75): one
 // thread per request walks them so every value rounds as in the reference.
-// The plane's fields are read into registers first: the table stores could
-// alias the request record as far as the compiler knows, which made it
-// reload them on every iteration (~300 cycles per column).
+// Only the two recurrences run here (one FP64 multiply and one add per
+// column: an FP64 instruction holds the SM sub-partition's FP64 pipe for
+// ~64 cycles on GB300, so the sequential thread is set by their count); the
+// running sum goes to along_center and plane_across_kernel turns it into
+// the centre, acc - size / 2 (the halving is exact, one rounding as before).
 __global__ void plane_along_kernel(const JshRequest* __restrict__ reqs) {
   if (threadIdx.x != 0) return;
   const JshPlane& p = reqs[blockIdx.x].plane;
@@ -31,17 +33,20 @@ __global__ void plane_along_kernel(const JshRequest* __restrict__ reqs) {
   for (uint64_t j = 0; j < n; ++j) {
     size[j] = cur;
     acc = (j == 0) ? cur : ad(acc, cur);
-    center[j] = sb(acc, ml(0.5, cur));
+    center[j] = acc;
     cur = ml(cur, base);
   }
 }
 
 // Column j of the across table: partial sums of n_across/2 copies of the
-// column's pixel size, minus half a size (src/Image.cpp:110-126).
+// column's pixel size, minus half a size (src/Image.cpp:110-126); and the
+// column's centre along the plane, its running size sum minus half its size
+// (src/Image.cpp:70-75).
 __global__ void plane_across_kernel(const JshRequest* __restrict__ reqs) {
   const JshPlane& p = reqs[blockIdx.y].plane;
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.n_along) return;
+  p.along_center[j] = sb(p.along_center[j], ml(0.5, p.along_size[j]));
   uint64_t nh = p.n_across / 2, na = p.n_along;
   double* __restrict__ pos = p.across_pos;
   double s = ml(p.along_size[j], 1.0);
