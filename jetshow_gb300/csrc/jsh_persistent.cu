@@ -168,19 +168,22 @@ struct Lane {
   uint32_t evals0;       // split form, IQUV kernel: the item's tau-pass evaluations (cost map)
 };
 
-// Stage derivatives of this thread: shared[(s * NK + c) * blockDim + tid].
-template <int NK>
+// Stage derivatives of this thread, thread-major: t[s * NK + c] with t =
+// shared + tid * W.  Every access is a compile-time offset from one base
+// register (no per-access address arithmetic), and W = 35 or 7 floats maps
+// a warp's 32 threads onto 32 distinct banks (W odd).  W is the per-thread
+// region of the kernel's buffer, so a one-component view of a 5-component
+// buffer (the single-kernel form's tau lanes) stays inside its own thread.
+template <int NK, int W = 7 * NK>
 struct Stages {
-  float* sh;
-  __device__ __forceinline__ float& operator()(int s, int c) const {
-    return sh[(s * NK + c) * blockDim.x + threadIdx.x];
-  }
+  float* t;
+  __device__ __forceinline__ float& operator()(int s, int c) const { return t[s * NK + c]; }
 };
 
 // acc = sum_{j < S} a_Sj K_j with S and j compile-time: the tableau entries
 // are immediate operands and the S*NK shared loads are independent.
-template <int S, int NK>
-__device__ __forceinline__ void combine_stage(const Stages<NK>& K, float* acc) {
+template <int S, int NK, int W>
+__device__ __forceinline__ void combine_stage(const Stages<NK, W>& K, float* acc) {
 #pragma unroll
   for (int c = 0; c < NK; ++c) acc[c] = 0.f;
 #pragma unroll
@@ -190,15 +193,15 @@ __device__ __forceinline__ void combine_stage(const Stages<NK>& K, float* acc) {
   }
 }
 
-template <int NK>
-__device__ __forceinline__ void combine(int s, const Stages<NK>& K, float* acc) {
+template <int NK, int W>
+__device__ __forceinline__ void combine(int s, const Stages<NK, W>& K, float* acc) {
   switch (s) {
-    case 1: combine_stage<1, NK>(K, acc); break;
-    case 2: combine_stage<2, NK>(K, acc); break;
-    case 3: combine_stage<3, NK>(K, acc); break;
-    case 4: combine_stage<4, NK>(K, acc); break;
-    case 5: combine_stage<5, NK>(K, acc); break;
-    default: combine_stage<6, NK>(K, acc); break;
+    case 1: combine_stage<1, NK, W>(K, acc); break;
+    case 2: combine_stage<2, NK, W>(K, acc); break;
+    case 3: combine_stage<3, NK, W>(K, acc); break;
+    case 4: combine_stage<4, NK, W>(K, acc); break;
+    case 5: combine_stage<5, NK, W>(K, acc); break;
+    default: combine_stage<6, NK, W>(K, acc); break;
   }
 }
 
@@ -913,8 +916,8 @@ abort:
 // quadrature panel's error estimate can miss a jump between its nodes).
 // dtau/dt = k_I does not depend on the state, so only the last stage
 // combination (the increment) is formed.
-template <int PASS, bool GENERAL>
-__device__ __forceinline__ void tau_dopri_step(Lane& L, const JshRequest* __restrict__ reqs, const Stages<1>& K,
+template <int PASS, bool GENERAL, int W>
+__device__ __forceinline__ void tau_dopri_step(Lane& L, const JshRequest* __restrict__ reqs, const Stages<1, W>& K,
                                                int part, Tally& T) {
   const JshRequest& R = reqs[L.r];
   const JshFreqConst F = R.mix.fc[L.f];
@@ -958,7 +961,7 @@ __device__ __forceinline__ void tau_dopri_step(Lane& L, const JshRequest* __rest
     for (int s = 1; s < 7; ++s) {
       if (s == 6) {
         float acc[1];
-        combine<1>(6, K, acc);
+        combine<1, W>(6, K, acc);
         inc = h * acc[0];
       }
       Coef32 c;
@@ -1068,11 +1071,11 @@ abort:
 // benchmark family (helical conical B and BK n in the plasma frame, flat
 // flow), a Dormand-Prince attempt otherwise.  The choice belongs to the
 // request, so every build of the kernels gives the same bits.
-template <int PASS, bool GENERAL>
-__device__ __forceinline__ void tau_step(Lane& L, const JshRequest* __restrict__ reqs, const Stages<1>& K1, int part,
-                                         Tally& T) {
+template <int PASS, bool GENERAL, int W>
+__device__ __forceinline__ void tau_step(Lane& L, const JshRequest* __restrict__ reqs, const Stages<1, W>& K1,
+                                         int part, Tally& T) {
   if (!GENERAL || reqs[L.r].mix.helical_log) tau_panel_step<PASS, GENERAL>(L, reqs, part, T);
-  else tau_dopri_step<PASS, GENERAL>(L, reqs, K1, part, T);
+  else tau_dopri_step<PASS, GENERAL, W>(L, reqs, K1, part, T);
 }
 
 // ------------------------------------------------------- I / IQUV pass
@@ -1269,7 +1272,8 @@ abort:
 template <bool FULL, int PASS, bool GENERAL = true>
 __device__ __forceinline__ void lane_advance(Lane& L, const JshRequest* __restrict__ reqs,
                                              const Stages<StageWidth<FULL>::NK>& K, Tally& T, int part = 0) {
-  if (PASS == PASS_BOTH && L.phase == PH_TAU) tau_step<PASS, GENERAL>(L, reqs, Stages<1>{K.sh}, part, T);
+  if (PASS == PASS_BOTH && L.phase == PH_TAU)
+    tau_step<PASS, GENERAL, 7 * StageWidth<FULL>::NK>(L, reqs, Stages<1, 7 * StageWidth<FULL>::NK>{K.t}, part, T);
   else lane_step<FULL, PASS, GENERAL>(L, reqs, K, T);
 }
 
@@ -1357,7 +1361,7 @@ __global__ void __launch_bounds__(128) transfer_static_mixed_kernel(const JshReq
   extern __shared__ float ksh[];
   batch_prefix(reqs, n_req, base);
   const unsigned long long w = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const Stages<FULL ? 5 : 1> K{ksh};
+  const Stages<FULL ? 5 : 1> K{ksh + threadIdx.x * (FULL ? 35 : 7)};
   Tally T = tally_new();
   if (w < base[n_req]) {
     Lane L;
@@ -1380,7 +1384,7 @@ __global__ void __launch_bounds__(COMPACT ? 128 : 256, COMPACT ? 3 : 1)
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
   extern __shared__ float ksh[];
   batch_prefix(reqs, n_req, base);
-  const Stages<FULL ? 5 : 1> K{ksh};
+  const Stages<FULL ? 5 : 1> K{ksh + threadIdx.x * (FULL ? 35 : 7)};
   const unsigned long long total = base[n_req];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -1448,7 +1452,7 @@ __global__ void __launch_bounds__(256, GENERAL ? 2 : 3) transfer_tau_kernel(cons
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
   extern __shared__ float ksh[];
   tau_prefix(reqs, n_req, part, base);
-  const Stages<1> K1{ksh};
+  const Stages<1> K1{ksh + threadIdx.x * 7};
   const unsigned long long total = base[n_req];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -1549,7 +1553,7 @@ __global__ void __launch_bounds__(COMPACT ? 128 : 256, COMPACT ? 3 : 1)
   __shared__ unsigned long long base[JSH_MAX_BATCH + 1];
   extern __shared__ float ksh[];
   iquv_prefix(reqs, n_req, part, base);
-  const Stages<FULL ? 5 : 1> K{ksh};
+  const Stages<FULL ? 5 : 1> K{ksh + threadIdx.x * (FULL ? 35 : 7)};
   const unsigned long long total = base[n_req];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
