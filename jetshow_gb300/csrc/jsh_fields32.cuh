@@ -48,10 +48,37 @@ struct GridW {
   float w0, w1, w2;
   bool ok;
 };
-__device__ inline GridW grid_locate32(const JshGrid& G, float px, float py) {
+// Barycentric weights of (px, py) in triangle t; true when inside (the
+// -1e-6 tolerance of the bucket search).
+__device__ __forceinline__ bool grid_tri32(const JshGrid& G, int t, float px, float py, GridW& g) {
+  const int v0 = G.tri[3 * t], v1 = G.tri[3 * t + 1], v2 = G.tri[3 * t + 2];
+  const float2 a = *reinterpret_cast<const float2*>(G.xyf + 2 * v0);
+  const float2 bb = *reinterpret_cast<const float2*>(G.xyf + 2 * v1);
+  const float2 c = *reinterpret_cast<const float2*>(G.xyf + 2 * v2);
+  const float area = (bb.x - a.x) * (c.y - a.y) - (bb.y - a.y) * (c.x - a.x);
+  if (area == 0.f) return false;
+  const float ia = 1.f / area;
+  const float w0 = ((bb.x - px) * (c.y - py) - (bb.y - py) * (c.x - px)) * ia;
+  const float w1 = ((px - a.x) * (c.y - a.y) - (py - a.y) * (c.x - a.x)) * ia;
+  const float w2 = 1.f - w0 - w1;
+  if (w0 >= -1e-6f && w1 >= -1e-6f && w2 >= -1e-6f) {
+    g = GridW{v0, v1, v2, w0, w1, w2, true};
+    return true;
+  }
+  return false;
+}
+
+// Point location of (px, py).  `hint` (may be null): the triangle of the
+// lane's previous evaluation, tried first -- consecutive evaluation points
+// along a ray mostly fall in the same triangle, and the bucket search costs
+// a chain of dependent loads per candidate (bucket, list, triangle,
+// vertices); the found triangle is stored back.  The hint restarts with
+// each item, so an item's lookups do not depend on the lane that runs it.
+__device__ inline GridW grid_locate32(const JshGrid& G, float px, float py, int* hint = nullptr) {
   GridW g;
   g.ok = false;
   if (G.n_tri == 0) return g;
+  if (hint && *hint >= 0 && grid_tri32(G, *hint, px, py, g)) return g;
   const float fx = (px - G.x0f) * G.inv_hf, fy = (py - G.y0f) * G.inv_hf;
   if (!(fx >= 0.f && fy >= 0.f)) return g;
   const int i = min((int)fx, G.nbx - 1), j = min((int)fy, G.nby - 1);
@@ -59,18 +86,8 @@ __device__ inline GridW grid_locate32(const JshGrid& G, float px, float py) {
   const int q1 = G.bstart[b + 1];
   for (int q = G.bstart[b]; q < q1; ++q) {
     const int t = G.bitems[q];
-    const int v0 = G.tri[3 * t], v1 = G.tri[3 * t + 1], v2 = G.tri[3 * t + 2];
-    const float2 a = *reinterpret_cast<const float2*>(G.xyf + 2 * v0);
-    const float2 bb = *reinterpret_cast<const float2*>(G.xyf + 2 * v1);
-    const float2 c = *reinterpret_cast<const float2*>(G.xyf + 2 * v2);
-    const float area = (bb.x - a.x) * (c.y - a.y) - (bb.y - a.y) * (c.x - a.x);
-    if (area == 0.f) continue;
-    const float ia = 1.f / area;
-    const float w0 = ((bb.x - px) * (c.y - py) - (bb.y - py) * (c.x - px)) * ia;
-    const float w1 = ((px - a.x) * (c.y - a.y) - (py - a.y) * (c.x - a.x)) * ia;
-    const float w2 = 1.f - w0 - w1;
-    if (w0 >= -1e-6f && w1 >= -1e-6f && w2 >= -1e-6f) {
-      g = GridW{v0, v1, v2, w0, w1, w2, true};
+    if (grid_tri32(G, t, px, py, g)) {
+      if (hint) *hint = t;
       return g;
     }
   }
@@ -430,13 +447,15 @@ __device__ __forceinline__ void coef32_helical_log(const JshMixed& X, const JshF
 }
 
 // (rk_h, rk_f, rk_e): hit index, frequency and evaluation index of the
-// per-evaluation random direction (JSH_RND_POINTS only).
+// per-evaluation random direction (JSH_RND_POINTS only); tri_hint: the
+// lane's point-location hint for fields on one shared grid (may be null).
 // GENERAL = false compiles the fused benchmark-family path alone, for
 // kernels launched only on requests whose mix.helical_log is set (the same
 // arithmetic as the general build takes for them).
 template <bool GENERAL = true>
 __device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqConst& F, F3 p, int mode, Coef32& c,
-                                          uint32_t rk_h = 0, uint32_t rk_f = 0, uint32_t rk_e = 0) {
+                                          uint32_t rk_h = 0, uint32_t rk_f = 0, uint32_t rk_e = 0,
+                                          int* tri_hint = nullptr) {
   const JshModel& m = R.model;
   const JshMixed& X = R.mix;
   if (!GENERAL || X.helical_log) {
@@ -474,7 +493,7 @@ __device__ __forceinline__ void coef32_rt(const JshRequest& R, const JshFreqCons
   } else if (X.sim_shared) {
     // every field from one grid (the simulation workload): one point location
     // for Gamma, n, B_p and B_phi
-    const GridW g = grid_locate32(m.grids[0], p.z, sqrtf(p.x * p.x + p.y * p.y));
+    const GridW g = grid_locate32(m.grids[0], p.z, sqrtf(p.x * p.x + p.y * p.y), tri_hint);
     gamma = grid_val32(m.grids[0], g, m.f_v, 1.0f);
     vdir = f3(0, 0, 1);
     kinematics32(gamma, vdir, f3(X.nl[0], X.nl[1], X.nl[2]), D, nlp, beta);

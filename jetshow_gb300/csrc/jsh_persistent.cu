@@ -166,6 +166,7 @@ struct Lane {
   uint32_t status;
   uint32_t evals, acc, rej;
   uint32_t evals0;       // split form, IQUV kernel: the item's tau-pass evaluations (cost map)
+  int32_t tri;           // gridded fields on one grid: triangle of the last evaluation (-1: none)
 };
 
 // Stage derivatives of this thread, thread-major: t[s * NK + c] with t =
@@ -323,6 +324,7 @@ __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict
   L.x[0] = L.x[1] = L.x[2] = L.x[3] = 0.f;
   L.status = (uint32_t)H.status | JSH_ST_HIT;
   L.evals = L.acc = L.rej = 0;
+  L.tri = -1;
   L.evals0 = 0;
   begin_tau_segment(L, R, H);
 }
@@ -488,9 +490,9 @@ __device__ __noinline__ double crossing_time(double tau_old, double t_old, doubl
 template <bool GENERAL>
 __device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& F, bool full, F3 p, const float* y,
                                        float cs, float sn, float* dk, float& kI, uint32_t rk_h, uint32_t rk_f,
-                                       uint32_t rk_e) {
+                                       uint32_t rk_e, int* tri) {
   Coef32 c;
-  coef32_rt<GENERAL>(R, F, p, full ? COEF_FULL : COEF_I, c, rk_h, rk_f, rk_e);
+  coef32_rt<GENERAL>(R, F, p, full ? COEF_FULL : COEF_I, c, rk_h, rk_f, rk_e, tri);
   kI = c.kI;
   const float scale = fabsf(c.eI) + fabsf(c.kI * y[0]);
   if (!full) {
@@ -589,6 +591,7 @@ __device__ __forceinline__ void lane_start_iquv(Lane& L, const JshRequest* __res
   L.status = it.status;
   L.evals0 = it.evals;
   L.evals = L.acc = L.rej = 0;
+  L.tri = -1;
   L.seg = L.first_seg >= 0 ? L.first_seg : L.nseg - 1;
   const JshHit& H = R.hits[L.h];
   if (eq) {
@@ -697,6 +700,7 @@ __device__ __forceinline__ void tau_pass_done(Lane& L, const JshRequest* __restr
     return;
   }
   L.seg = L.first_seg >= 0 ? L.first_seg : L.nseg - 1;
+  L.tri = -1;  // as the IQUV kernel's fresh lanes
   const JshHit& H = R.hits[L.h];
   if (eq) {
     const int s = L.seg;
@@ -950,7 +954,7 @@ __device__ __forceinline__ void tau_dopri_step(Lane& L, const JshRequest* __rest
     const float h = L.dt;
     if (!L.init) {
       Coef32 c;
-      coef32_rt<GENERAL>(R, F, pn, COEF_KI, c, L.h, (uint32_t)L.f, L.evals);
+      coef32_rt<GENERAL>(R, F, pn, COEF_KI, c, L.h, (uint32_t)L.f, L.evals, &L.tri);
       L.k1[0] = c.kI;
       L.evals++;
       L.init = true;
@@ -966,7 +970,7 @@ __device__ __forceinline__ void tau_dopri_step(Lane& L, const JshRequest* __rest
       }
       Coef32 c;
       coef32_rt<GENERAL>(R, F, pn + dirf * (c_C[s] * h), COEF_KI, c, L.h, (uint32_t)L.f,
-                         L.evals + (uint32_t)(s - 1));
+                         L.evals + (uint32_t)(s - 1), &L.tri);
       K(s, 0) = c.kI;
     }
     L.evals += 6;
@@ -1116,7 +1120,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     const float h = L.dt;
     float dk[5];
     if (!L.init) {
-      L.s1 = rhs32<GENERAL>(R, F, FULL, pn, L.x, c0, s0, dk, L.kI1, L.h, (uint32_t)L.f, L.evals0 + L.evals);
+      L.s1 = rhs32<GENERAL>(R, F, FULL, pn, L.x, c0, s0, dk, L.kI1, L.h, (uint32_t)L.f, L.evals0 + L.evals, &L.tri);
 #pragma unroll
       for (int c = 0; c < NK; ++c) L.k1[c] = dk[c];
       L.evals++;
@@ -1141,7 +1145,7 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
         sn = s0 * cd + c0 * sd;
       }
       const float sc = rhs32<GENERAL>(R, F, FULL, pn + dirf * (c_C[s] * h), y, cs, sn, dk, kI7, L.h, (uint32_t)L.f,
-                                      L.evals0 + L.evals + (uint32_t)(s - 1));
+                                      L.evals0 + L.evals + (uint32_t)(s - 1), &L.tri);
       smax = fmaxf(smax, sc);
       s7 = sc;
 #pragma unroll
