@@ -1230,6 +1230,32 @@ int jo_coefficients(const jsh_model_desc* model, const double* point, const doub
   return JSH_OK;
 }
 
+/* The field laws at a lab-frame point [cm]: out = {B (the vector; a scalar
+ * law's |B| in out[0], 0, 0), n, v (3) [cm/s]} (BField::bf, NField::nf,
+ * VField::vf of src/BField.cpp, src/NField.cpp, src/VField.cpp); for the
+ * known-answer tests of the laws. */
+int jo_fields(const jsh_model_desc* model, const double* point, double* out) {
+  model_t m;
+  int st = model_init(model, &m);
+  if (st) return st;
+  const v3 p = mk(point[0], point[1], point[2]);
+  if (m.b_scalar) {
+    out[0] = bscalar(&m, p);
+    out[1] = out[2] = 0.0;
+  } else {
+    const v3 b = bvector(&m, p);
+    out[0] = b.x;
+    out[1] = b.y;
+    out[2] = b.z;
+  }
+  out[3] = nfield(&m, p);
+  const v3 v = vfield(&m, p);
+  out[4] = v.x;
+  out[5] = v.y;
+  out[6] = v.z;
+  return JSH_OK;
+}
+
 /* ====================================================================
  * Dormand-Prince 5(4) with dense output and odeint-documented control.
  * ==================================================================== */
@@ -1427,6 +1453,8 @@ static int steps_schedule(double tau, int n_min, int n_max) {
   double n = k * pow((log(tau) + b), 2.0) + n_min;
   return (int)ceil(n);
 }
+
+int jo_steps_schedule(double tau, int n_min, int n_max) { return steps_schedule(tau, n_min, n_max); }
 
 typedef struct {
   double tau, l, iquv[4];

@@ -57,6 +57,15 @@ void jo_set_item_evals(uint64_t* buf);
 int jo_coefficients(const jsh_model_desc* model, const double* point,
                     const double* n_los, double nu, double* out);
 
+/* The field laws at a lab-frame point [cm]: out = {B (a scalar law's |B| in
+ * out[0]), n, v [cm/s]}. */
+int jo_fields(const jsh_model_desc* model, const double* point, double* out);
+
+/* steps_schedule (src/utils.cpp:354-366) with the limits the I pass gives
+ * it (tau_n_min 0.1, tau_n_max 100): the divisor of a segment's first step
+ * by the background optical depth. */
+int jo_steps_schedule(double tau, int n_min, int n_max);
+
 /* Integrate dx/dt = a x + b (scalar) from 0 to L with the tau-pass machinery
  * (dense-output Dormand-Prince, odeint adaptive-range semantics) and return
  * x(L); used by the known-answer tests of the integrator. */

@@ -52,6 +52,9 @@ def lib():
         L.jo_render.argtypes = [P(A.ModelDesc), P(A.PlaneDesc), D, C.c_int32, P(A.Params),
                                 P(C.c_int64), C.c_int64, C.c_int32, P(A.Image), P(Counters)]
         L.jo_coefficients.argtypes = [P(A.ModelDesc), D, D, C.c_double, D]
+        L.jo_fields.argtypes = [P(A.ModelDesc), D, D]
+        L.jo_steps_schedule.argtypes = [C.c_double, C.c_int, C.c_int]
+        L.jo_steps_schedule.restype = C.c_int
         L.jo_test_linear_dense.argtypes = [C.c_double] * 6 + [P(C.c_int64)]
         L.jo_test_linear_dense.restype = C.c_double
         L.jo_test_linear_controlled.argtypes = [C.c_double] * 6 + [P(C.c_int64)]
@@ -140,6 +143,15 @@ def coefficients(model, point, n_los, nu):
     p = np.ascontiguousarray(point, dtype=np.float64)
     n = np.ascontiguousarray(n_los, dtype=np.float64)
     _chk(lib().jo_coefficients(C.byref(model), A.dptr(p), A.dptr(n), nu, A.dptr(out)))
+    return out
+
+
+def fields(model, point):
+    """B (3; a scalar law's |B| first), n and v (3) [cm/s] of the model's
+    laws at a lab-frame point [cm]."""
+    out = np.zeros(7)
+    p = np.ascontiguousarray(point, dtype=np.float64)
+    _chk(lib().jo_fields(C.byref(model), A.dptr(p), A.dptr(out)))
     return out
 
 
