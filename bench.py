@@ -85,6 +85,10 @@ def parse():
                     help="requests of the replayed serving stream (0 skips the serving leg)")
     ap.add_argument("--saturate-rate", type=float, default=5000.0,
                     help="arrival rate [1/s] of a second replay that saturates the device (0 skips it)")
+    ap.add_argument("--sustain-rate", type=float, default=40.0,
+                    help="arrival rate [1/s] of a third replay the device carries (0 skips it)")
+    ap.add_argument("--sustain-requests", type=int, default=400,
+                    help="requests of the sustainable-rate replay")
     ap.add_argument("--no-configs", dest="configs", action="store_false",
                     help="skip the C0 and C2 legs")
     return ap.parse_args()
@@ -608,11 +612,13 @@ def main():
                        "tau_evals_per_step": int(n_tau), "iquv_evals_per_step": int(n_iquv)},
             "fp64_peak_tflops": peaks["fp64_tflops"]}
     cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 and conical else None
-    serving = saturated = None
+    serving = saturated = sustained = None
     if args.serve_requests > 0:
         serving = serving_leg(ctx, args.serve_requests)
         if args.saturate_rate > 0:
             saturated = serving_leg(ctx, args.serve_requests, rate_hz=args.saturate_rate, warm=False)
+        if args.sustain_rate > 0 and args.sustain_requests > 0:
+            sustained = serving_leg(ctx, args.sustain_requests, rate_hz=args.sustain_rate, warm=False)
     gridded = gridded_leg(ctx) if args.gridded else None
     configs = None
     if args.configs and conical and rank == 0:
@@ -638,7 +644,8 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": float(np.mean(e2e_ms))},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
-                "serving_saturated": saturated, "gridded": gridded, "configs": configs,
+                "serving_saturated": saturated, "serving_sustainable": sustained, "gridded": gridded,
+                "configs": configs,
                 "gpu_launches": int(st_b["kernels_launched"]) * args.steps,
                 "gpu_launches_per_step": ({"plane": 2, "hit": 1, "rank": 3, "tau": 2, "iquv_rank": 6, "iquv": 2}
                                           if st_b["kernels_launched"] == 15 else
