@@ -435,11 +435,19 @@ def config_leg(R, jet, plane, nu, kw, steps, plain_scale, plain_builder, n_err_p
     (device time), the plain all-FP64 form on the same model at
     ``plain_scale`` (a coarser plane of the same extent: the bounded
     subset), errors of the batched form against the converged oracle on a
-    random sample plus the ``n_deep`` deepest pixels, and the core Faraday
-    depth at the lowest frequency when asked."""
+    random sample plus the ``n_deep`` deepest pixels, and, when asked, the
+    core Faraday depth at the lowest frequency and the batched form with the
+    Faraday-thick mode (JSH_FLAG_FARADAY_THICK; its errors on the same
+    pixels)."""
     from jetshow_gb300 import jet as J
+    from jetshow_gb300 import _capi as A
     model, pdesc = jet.desc(), plane.desc()
     npix = plane.image_size[0] * plane.image_size[1]
+    out_f = None
+    if faraday:
+        ms_f, st_f = R.timed(model, pdesc, nu, J.make_params(precision="mixed", schedule="persistent",
+                                                             flags=A.FLAG_FARADAY_THICK, **kw), steps, 1)
+        out_f = R.host(nu.size, npix)
     p_b = J.make_params(precision="mixed", schedule="persistent", **kw)
     ms_b, st_b = R.timed(model, pdesc, nu, p_b, steps, 1)
     out_b = R.host(nu.size, npix)
@@ -447,6 +455,10 @@ def config_leg(R, jet, plane, nu, kw, steps, plain_scale, plain_builder, n_err_p
            "work_items": int(st_b["n_work_items"]), "batched": {
                "rays_per_s": st_b["n_work_items"] / (np.mean(ms_b) * 1e-3), "ms": float(np.mean(ms_b)),
                "rhs_evals": int(st_b["rhs_evals"]), "status_or": int(st_b["status_or"])}}
+    if faraday:
+        leg["batched_faraday_thick_mode"] = {
+            "rays_per_s": st_f["n_work_items"] / (np.mean(ms_f) * 1e-3), "ms": float(np.mean(ms_f)),
+            "rhs_evals": int(st_f["rhs_evals"]), "status_or": int(st_f["status_or"])}
     jp, plp, nup, _ = plain_builder(plain_scale)
     ms_p, st_p = R.timed(jp.desc(), plp.desc(), nup, J.make_params(precision="fp64", schedule="static", **kw), 1, 0)
     leg["plain_fp64"] = {"rays_per_s": st_p["n_work_items"] / (np.mean(ms_p) * 1e-3), "ms": float(np.mean(ms_p)),
@@ -456,8 +468,9 @@ def config_leg(R, jet, plane, nu, kw, steps, plain_scale, plain_builder, n_err_p
     tau0 = np.where((out_b["status"][0] & 1) != 0, out_b["tau"][0], -1.0)
     deep = np.argsort(tau0)[::-1][:n_deep]
     leg["deepest_tau"] = float(tau0[deep[0]])
-    leg["err_vs_converged_oracle"] = errors_vs_converged(jet, plane, nu, {"batched": out_b}, n_pix=n_err_pix,
-                                                         extra_pix=deep)
+    leg["err_vs_converged_oracle"] = errors_vs_converged(jet, plane, nu, {"batched": out_b,
+                                                                          "batched_faraday_thick_mode": out_f},
+                                                         n_pix=n_err_pix, extra_pix=deep)
     if faraday:
         leg["core_faraday_depth_rad"] = faraday_depth(jet, plane, float(nu[0]), int(deep[0]))
     return leg

@@ -282,6 +282,17 @@ typedef struct jsh_params {
  * Results are bitwise the same either way. */
 #define JSH_FLAG_SERIAL_PASSES 0x40
 #define JSH_FLAG_OVERLAP_PASSES 0x80
+/* Mixed precision, full Stokes: the Faraday-thick mode of the I/IQUV pass.
+ * Where Faraday rotation outruns absorption a hundredfold (|k_F| >= 100 k_I)
+ * the pass follows (Q, U) at its quasi-static value S / (k_I - i k_F) plus a
+ * decaying transient and steps on I and V alone, within the request's
+ * rtol/atol relative to I; it returns to the full integration where the
+ * adiabatic condition fails, near the jet axis and where k_F changes sign.
+ * Faraday-thick jet cores take thousands of times fewer steps.  The request
+ * runs kernels built with the mode (the default kernels leave its
+ * bookkeeping out); images of jets without Faraday-thick rays are the same
+ * to the last bit either way.  The FP64 path never uses it. */
+#define JSH_FLAG_FARADAY_THICK 0x100
 
 /* Fill *p with the reference's hard-coded values (src/pyjetshow.cpp:143-156,
  * src/Observation.cpp:156, :269): n = 100, tau_max = 1e4, tau_min = 1e-10,

@@ -37,6 +37,7 @@ FLAG_GENERAL_KERNELS = 0x10
 FLAG_KERNEL_TIMES = 0x20
 FLAG_SERIAL_PASSES = 0x40
 FLAG_OVERLAP_PASSES = 0x80
+FLAG_FARADAY_THICK = 0x100
 ST_ERRORS = ST_STEP_LIMIT | ST_FAIL_LIMIT | ST_BISECT_LIMIT | ST_NAN | ST_DT_UNDERFLOW
 
 GEO_CONE, GEO_CYLINDER, GEO_PARABALOID, GEO_PARABALOID_CONE, GEO_SIMULATION = 1, 2, 3, 4, 5

@@ -23,7 +23,8 @@ OUT = os.path.join(HERE, "_build")
 REPO = os.path.dirname(HERE)
 LIB = os.path.join(OUT, "libjetshow_gb300.so")
 
-CU_SOURCES = ["jsh_kernels.cu", "jsh_fp64.cu", "jsh_persistent.cu", "jsh_noalloc.cu", "jsh_stripe.cu", "jsh_visibility.cu"]
+CU_SOURCES = ["jsh_kernels.cu", "jsh_fp64.cu", "jsh_persistent.cu", "jsh_persistent_ft.cu", "jsh_noalloc.cu", "jsh_stripe.cu",
+              "jsh_visibility.cu"]
 CPP_SOURCES = ["jsh_host.cpp", "jsh_capi.cpp", "jsh_server.cpp", "jsh_autotune.cpp", "jsh_grid.cpp", "jsh_hull.cpp", "jsh_cells.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Units whose kernels must round identically in every instantiation: the
@@ -31,7 +32,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # persistent, split tau and IQUV kernels) whose images are bitwise equal
 # only if the compiler fuses no multiply-add on its own (the explicit fmaf
 # calls stay fused).
-NO_CONTRACT = {"jsh_persistent.cu"}
+NO_CONTRACT = {"jsh_persistent.cu", "jsh_persistent_ft.cu"}
+# Sources that include another source file.
+INCLUDED = {"jsh_persistent_ft.cu": ["jsh_persistent.cu"]}
 
 
 def _cuda_home() -> str:
@@ -73,7 +76,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
                "-Xptxas", "-v", "-Xcompiler", "-fPIC,-ffp-contract=off", *inc, "-c", s, "-o", o]
         if src in NO_CONTRACT:
             cmd.insert(1, "--fmad=false")
-        jobs.append((o, [s, *headers], cmd))
+        jobs.append((o, [s, *headers, *(os.path.join(CSRC, f) for f in INCLUDED.get(src, []))], cmd))
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT, src + ".o")

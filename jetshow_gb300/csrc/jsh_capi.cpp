@@ -150,6 +150,7 @@ JshLaunchShape jsh_params_shape(JshLaunchShape s, const jsh_params* params) {
   if (params->refill_threshold > 0) s.refill_threshold = params->refill_threshold;
   if (params->flags & JSH_FLAG_COMPACT_REGS) s.compact = 1;
   if (params->flags & JSH_FLAG_SINGLE_KERNEL) s.single = 1;
+  s.faraday_thick = (params->flags & JSH_FLAG_FARADAY_THICK) ? 1 : 0;
   if (s.block_size < 32) s.block_size = 32;
   if (s.block_size > 512) s.block_size = 512;
   s.block_size = s.block_size / 32 * 32;

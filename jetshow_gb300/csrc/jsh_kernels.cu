@@ -265,6 +265,11 @@ cudaError_t jsh_launch_transfer_persistent64(const JshRequest* d_reqs, int n_req
 cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int schedule, bool full,
                                       uint64_t max_items, uint64_t max_hits, const JshLaunchShape& shape,
                                       unsigned int* queue, int num_sms, cudaStream_t stream);
+// jsh_persistent_ft.cu: the same launch sequence over the kernels built with
+// the Faraday-thick mode
+cudaError_t jsh_launch_transfer_mixed_ft(const JshRequest* d_reqs, int n_req, int schedule, bool full,
+                                         uint64_t max_items, uint64_t max_hits, const JshLaunchShape& shape,
+                                         unsigned int* queue, int num_sms, cudaStream_t stream);
 
 cudaError_t jsh_launch_plane(const JshRequest* d_reqs, int n_req, uint64_t max_along, cudaStream_t stream) {
   if (n_req <= 0) return cudaSuccess;
@@ -288,8 +293,8 @@ cudaError_t jsh_launch_transfer(const JshRequest* d_reqs, int n_req, int precisi
                                 unsigned int* queue, int num_sms, cudaStream_t stream) {
   if (n_req <= 0 || max_items == 0) return cudaSuccess;
   if (precision == JSH_PREC_MIXED)
-    return jsh_launch_transfer_mixed(d_reqs, n_req, schedule, full, max_items, max_hits, shape, queue, num_sms,
-                                     stream);
+    return (full && shape.faraday_thick ? jsh_launch_transfer_mixed_ft : jsh_launch_transfer_mixed)(
+        d_reqs, n_req, schedule, full, max_items, max_hits, shape, queue, num_sms, stream);
   if (schedule == JSH_SCHED_PERSISTENT)
     return jsh_launch_transfer_persistent64(d_reqs, n_req, max_items, shape, queue, num_sms, stream);
   return jsh_launch_transfer_static64(d_reqs, n_req, max_items, stream);

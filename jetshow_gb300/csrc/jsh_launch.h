@@ -37,6 +37,9 @@ struct JshLaunchShape {
   int overlap_key;
   cudaStream_t side;
   cudaEvent_t* fork;
+  // mixed precision, full Stokes: run the kernels built with the
+  // Faraday-thick mode (JSH_FLAG_FARADAY_THICK)
+  int faraday_thick;
 };
 
 // Ray generation: along sizes and centres (sequential recurrence of

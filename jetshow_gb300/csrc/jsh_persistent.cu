@@ -97,6 +97,8 @@ __constant__ float c_E[7] = {(float)dp::E1, 0, (float)dp::E3, (float)dp::E4, (fl
                              (float)dp::E7};
 __constant__ float c_D[7] = {(float)dp::D1, 0, (float)dp::D3, (float)dp::D4, (float)dp::D5, (float)dp::D6,
                              (float)dp::D7};
+// 5th-order weights b of the first six stages (b_7 = 0)
+__constant__ float c_B[6] = {(float)dp::B1, 0, (float)dp::B3, (float)dp::B4, (float)dp::B5, (float)dp::B6};
 
 // Compensated FP32 pair x = hi + lo, |lo| <= ulp(hi) / 2 (about 48 bits):
 // the step-control state (segment coordinate, remainder, optical depth,
@@ -147,6 +149,9 @@ struct Lane {
   int8_t first_seg;      // segment where the IQUV pass starts inside (-1: at its end)
   bool init;
   bool last;             // dt was truncated to reach the segment's end
+  uint8_t ft;            // IQUV pass in the Faraday-thick mode (quasi-static polarisation)
+  uint8_t ft_cool;       // steps before the Faraday-thick mode may be tried again
+  uint8_t ft_back;       // entry estimates in a row that found the transient too large (back-off)
   DF p0x, p0y, p0z;      // segment start [pc]
   float bx, by, bz;      // p0 + t d rounded to FP32 after each accepted step:
                          // stage points are b + c h d in FP32 (error u |b|)
@@ -290,6 +295,9 @@ __device__ __forceinline__ void begin_iquv_segment(Lane& L, const JshRequest& R,
   }
   set_segment(L, ox, oy, oz, seg_len_cm(H, s, ox, oy, oz));
   L.dt = (L.length.hi + L.length.lo) / first_step_divisor(L.tau_bg, R.P.n);
+  L.ft = 0;  // (Q, U) enters a segment as it left the last one, not quasi-static
+  L.ft_cool = 0;
+  L.ft_back = 0;
 }
 
 // Work item w of the batch.  Unranked: frequency-major over the hit list.
@@ -325,6 +333,8 @@ __device__ __forceinline__ void lane_start(Lane& L, const JshRequest* __restrict
   L.status = (uint32_t)H.status | JSH_ST_HIT;
   L.evals = L.acc = L.rej = 0;
   L.tri = -1;
+  L.ft = 0;
+  L.ft_cool = 0;
   L.evals0 = 0;
   begin_tau_segment(L, R, H);
 }
@@ -490,7 +500,7 @@ __device__ __noinline__ double crossing_time(double tau_old, double t_old, doubl
 template <bool GENERAL>
 __device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& F, bool full, F3 p, const float* y,
                                        float cs, float sn, float* dk, float& kI, uint32_t rk_h, uint32_t rk_f,
-                                       uint32_t rk_e, int* tri) {
+                                       uint32_t rk_e, int* tri, bool ft = false, float* cpl = nullptr) {
   Coef32 c;
   coef32_rt<GENERAL>(R, F, p, full ? COEF_FULL : COEF_I, c, rk_h, rk_f, rk_e, tri);
   kI = c.kI;
@@ -498,6 +508,26 @@ __device__ __forceinline__ float rhs32(const JshRequest& R, const JshFreqConst& 
   if (!full) {
     dk[0] = c.eI - c.kI * y[0];
     dk[1] = dk[2] = dk[3] = dk[4] = 0.f;
+    return scale;
+  }
+  if (ft) {
+    // Faraday-thick mode: the lab-frame polarisation Pi = Q + iU obeys
+    // Pi' = -lambda Pi + S, lambda = k_I - i k_F, S = (eta_Q - k_Q I) - i k_C V.
+    // Where |lambda| is far above the rate at which S / lambda changes, Pi is
+    // that quasi-static value plus a transient d whose rotating-frame value
+    // only decays (d' = -k_I d, up to the adiabatic lag); I and V see the
+    // quasi-static part through k_Q Re Pi and k_C Im Pi, the transient's
+    // share rotates at k_F and integrates to at most ~cpl |d|.  dk[1], dk[2]
+    // carry the rotating-frame value e^{-i chi} S / lambda itself.
+    const float sre = c.eQ - c.kQ * y[0], sim = -c.kC * y[3];
+    const float il = 1.f / fmaf(c.kI, c.kI, c.kF * c.kF);
+    const float pre = fmaf(sre, c.kI, -sim * c.kF) * il, pim = fmaf(sre, c.kF, sim * c.kI) * il;
+    dk[0] = c.eI - c.kI * y[0] - c.kQ * pre - c.kV * y[3];
+    dk[1] = fmaf(cs, pre, sn * pim);
+    dk[2] = fmaf(-sn, pre, cs * pim);
+    dk[3] = c.eV - c.kI * y[3] - c.kV * y[0] + c.kC * pim;
+    dk[4] = c.kF;
+    *cpl = fmaxf(fabsf(c.kQ), fabsf(c.kC)) * sqrtf(il);
     return scale;
   }
   float Qlab = cs * y[1] - sn * y[2];
@@ -592,6 +622,8 @@ __device__ __forceinline__ void lane_start_iquv(Lane& L, const JshRequest* __res
   L.evals0 = it.evals;
   L.evals = L.acc = L.rej = 0;
   L.tri = -1;
+  L.ft = 0;
+  L.ft_cool = 0;
   L.seg = L.first_seg >= 0 ? L.first_seg : L.nseg - 1;
   const JshHit& H = R.hits[L.h];
   if (eq) {
@@ -612,6 +644,32 @@ __device__ __forceinline__ void lane_start_iquv(Lane& L, const JshRequest* __res
 // a Stokes component is about 0.3 u h scale (four terms of magnitude
 // <= scale per derivative, weighted by |e_j| <= 0.05).
 constexpr float kNoise = 5.9604645e-8f;
+// This file is compiled twice: as is, and by jsh_persistent_ft.cu with
+// JSH_FARADAY_THICK_BUILD 1 for requests that ask for the Faraday-thick mode
+// (JSH_FLAG_FARADAY_THICK).  The mode's bookkeeping in the step costs the
+// other requests ~18 % of the IQUV kernel even where it never engages, so
+// the default kernels are built without it.
+#ifndef JSH_FARADAY_THICK_BUILD
+#define JSH_FARADAY_THICK_BUILD 0
+#endif
+constexpr bool kFtm = JSH_FARADAY_THICK_BUILD != 0;
+// Faraday-thick mode of the IQUV pass: entry where
+// |k_F| >= kFtRatio k_I; the quasi-static part's lag and the transient's
+// left-out coupling must stay within kFtTol (atol + rtol I); after a refused
+// entry or an exit the mode waits kFtCooldown accepted steps, after an entry
+// estimate that found the transient too large kFtRetry, doubled for each
+// such estimate in a row (up to 255).
+constexpr float kFtRatio = 100.f;
+constexpr float kFtTol = 1.f;
+constexpr uint8_t kFtCooldown = 32;
+constexpr int kFtRetry = 16;  // accepted steps after an entry estimate that found the transient too large
+constexpr float kFtAxis = 0.25f;  // largest step / distance from the jet axis
+// The mode's tolerance scales with I, as the full mode's own control of
+// (Q, U) does through its noise floor (the quasi-static |Q + iU| is ~k_I/k_F
+// of I where the mode applies).
+__device__ __forceinline__ float ft_tolerance(float I, float rtol, float atol) {
+  return kFtTol * fmaf(rtol, fabsf(I), atol);
+}
 
 // Stage components of the I/IQUV pass's Dormand-Prince machine: the IQUV
 // state and chi (full Stokes) or I only.
@@ -701,6 +759,8 @@ __device__ __forceinline__ void tau_pass_done(Lane& L, const JshRequest* __restr
   }
   L.seg = L.first_seg >= 0 ? L.first_seg : L.nseg - 1;
   L.tri = -1;  // as the IQUV kernel's fresh lanes
+  L.ft = 0;
+  L.ft_cool = 0;
   const JshHit& H = R.hits[L.h];
   if (eq) {
     const int s = L.seg;
@@ -1099,6 +1159,23 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
   const float atol = F.atol;
   const float rtol = R.mix.rtol;
 
+  if (kFtm && FULL && L.ft) {
+    // Faraday-thick mode: its steps follow I and V only, so nothing else
+    // keeps them from straddling the narrow features of the field where a
+    // ray passes the jet axis (the dip of B_perp, the reversal of the
+    // azimuthal field within the approach distance): a step spans at most
+    // kFtAxis of the point's distance from the axis.  Where that is under a
+    // radian of rotation the full integration is as fast: leave the mode.
+    const float cap = kFtAxis * sqrtf(fmaf(L.bx, L.bx, L.by * L.by));
+    if (cap * fabsf(L.k1[NK - 1]) < 1.f) {
+      L.ft = 0;
+      L.ft_cool = kFtCooldown;
+      L.init = false;
+      L.dt = fminf(L.dt, 1.f / fabsf(L.k1[NK - 1]));
+    } else {
+      L.dt = fminf(L.dt, cap);
+    }
+  }
   // integrate_adaptive / adaptive range: finish at exactly t = length (a
   // step that would pass the end is shortened to end there)
   {
@@ -1118,13 +1195,27 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     float c0 = 1.f, s0 = 0.f;
     if (FULL) sincosf(L.chi.hi, &s0, &c0);
     const float h = L.dt;
-    float dk[5];
+    const bool ft = kFtm && FULL && L.ft;
+    float dk[5], cpl = 0.f;  // cpl: Faraday-thick mode, max(|k_Q|, |k_C|) / |lambda| of the last evaluation
     if (!L.init) {
-      L.s1 = rhs32<GENERAL>(R, F, FULL, pn, L.x, c0, s0, dk, L.kI1, L.h, (uint32_t)L.f, L.evals0 + L.evals, &L.tri);
+      L.s1 = rhs32<GENERAL>(R, F, FULL, pn, L.x, c0, s0, dk, L.kI1, L.h, (uint32_t)L.f, L.evals0 + L.evals, &L.tri,
+                            ft, &cpl);
 #pragma unroll
       for (int c = 0; c < NK; ++c) L.k1[c] = dk[c];
       L.evals++;
       L.init = true;
+      if (ft) {
+        // entry: the transient carried in, d = (q, u) - e^{-i chi} S / lambda,
+        // must be small enough that the rotating coupling the mode leaves
+        // out of I and V stays within the tolerance
+        const float dq = L.x[1] - dk[1], du = L.x[2] - dk[2];
+        if (!(cpl * sqrtf(fmaf(dq, dq, du * du)) <= ft_tolerance(L.x[0], rtol, atol))) {
+          L.ft = 0;
+          L.ft_cool = kFtCooldown;
+          L.init = false;
+          return;
+        }
+      }
     }
 #pragma unroll
     for (int c = 0; c < NK; ++c) K(0, c) = L.k1[c];
@@ -1145,9 +1236,19 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
         sn = s0 * cd + c0 * sd;
       }
       const float sc = rhs32<GENERAL>(R, F, FULL, pn + dirf * (c_C[s] * h), y, cs, sn, dk, kI7, L.h, (uint32_t)L.f,
-                                      L.evals0 + L.evals + (uint32_t)(s - 1), &L.tri);
+                                      L.evals0 + L.evals + (uint32_t)(s - 1), &L.tri, ft, &cpl);
       smax = fmaxf(smax, sc);
       s7 = sc;
+      if (ft && s < 6) {
+        // Faraday-thick mode: the inner stages' (q, u) slots are free (no
+        // stage point uses (q, u)); they keep the stage's k_I and its coupling
+        // factor, or +inf where rotation does not outrun absorption a
+        // hundredfold (a reversal of the line-of-sight field inside the step,
+        // as on rays past the axis of a helical field, breaks the
+        // quasi-static picture between the step's ends)
+        dk[2] = fabsf(dk[NK - 1]) >= kFtRatio * kI7 ? cpl : INFINITY;
+        dk[1] = kI7;
+      }
 #pragma unroll
       for (int c = 0; c < NK; ++c) K(s, c) = dk[c];
       if (s == 6) {
@@ -1188,11 +1289,46 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       const float fl_pol = (adt * fabsf(L.kI1) > 0.01f) ? 100.f * floor_ : floor_;
 #pragma unroll
       for (int c = 0; c < NX; ++c) {
+        if (ft && (c == 1 || c == 2)) continue;  // (Q, U) is not integrated in the Faraday-thick mode
         const float fl = (c == 0) ? floor_ : fl_pol;
         float r = fabsf(err[c]) / (fmaf(rtol, fmaf(adt, fabsf(L.k1[c]), fabsf(L.x[c])), atol) + fl);
         e = fmaxf(e, r);
       }
-      if (FULL) {
+      if (ft) {
+        // adiabatic condition of the quasi-static part: its lag behind
+        // S / lambda, (d/dt (S / lambda)) / lambda, estimated over the step
+        // from the lab-frame values at its ends, and the transient's left-out
+        // coupling stay within the tolerance; else the step is redone in the
+        // full mode (from the same state: (q, u) is the full polarisation in
+        // both modes)
+        float cs6, sn6;  // the frame at the step's end, as its last stage had it
+        {
+          float sd, cd;
+          __sincosf(inc[NK - 1], &sd, &cd);
+          cs6 = c0 * cd - s0 * sd;
+          sn6 = s0 * cd + c0 * sd;
+        }
+        float cpl_max = cpl;
+        bool ft_ok = fabsf(K(6, NK - 1)) >= kFtRatio * kI7;
+#pragma unroll
+        for (int j = 1; j < 6; ++j) cpl_max = fmaxf(cpl_max, K(j, 2));
+        ft_ok = ft_ok && cpl_max < INFINITY;
+        const float ft_tol = ft_tolerance(L.x[0], rtol, atol);
+        const float p0r = c0 * K(0, 1) - s0 * K(0, 2), p0i = s0 * K(0, 1) + c0 * K(0, 2);
+        const float p6r = cs6 * K(6, 1) - sn6 * K(6, 2), p6i = sn6 * K(6, 1) + cs6 * K(6, 2);
+        const float dr = p6r - p0r, di = p6i - p0i;
+        const float lam = sqrtf(fmaf(kI7, kI7, K(6, NK - 1) * K(6, NK - 1)));
+        const float dq = L.x[1] - K(0, 1), du = L.x[2] - K(0, 2);
+        if (!ft_ok || !(sqrtf(fmaf(dr, dr, di * di)) <= adt * lam * ft_tol) ||
+            !(cpl_max * sqrtf(fmaf(dq, dq, du * du)) <= ft_tol)) {
+          L.ft = 0;
+          L.ft_cool = kFtCooldown;
+          L.init = false;
+          L.dt = fminf(h, 1.f / fabsf(L.k1[NK - 1]));
+          return;
+        }
+      }
+      if (FULL && !ft) {
         // a rotation error d chi moves (Q, U) by P d chi; the lab-frame norm
         // of the reference would compare that with rtol (P + h |dQ/dt|),
         // and |dQ/dt| ~ k_F P there
@@ -1231,8 +1367,23 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
       float ee = e > 0.00032f ? e : 0.00032f;
       L.dt = h * (0.9f * __powf(ee, -0.2f));
     }
+    float qn = 0.f, un = 0.f;
+    if (ft) {
+      // quasi-static part at the end plus the transient, decayed by the
+      // step's optical depth (h sum b_j k_I,j over the stages)
+      float btau = c_B[0] * L.kI1;
+#pragma unroll
+      for (int j = 1; j < 6; ++j) btau = fmaf(c_B[j], K(j, 1), btau);
+      const float decay = expf(-h * btau);
+      qn = fmaf(L.x[1] - K(0, 1), decay, K(6, 1));
+      un = fmaf(L.x[2] - K(0, 2), decay, K(6, 2));
+    }
 #pragma unroll
     for (int c = 0; c < NX; ++c) L.x[c] += inc[c];
+    if (ft) {
+      L.x[1] = qn;
+      L.x[2] = un;
+    }
     if (FULL) {
       L.chi = df_add(L.chi, inc[NK - 1]);
       if (fabsf(L.chi.hi) > 3.14159265f) {
@@ -1247,6 +1398,34 @@ __device__ __forceinline__ void lane_step(Lane& L, const JshRequest* __restrict_
     for (int c = 0; c < NK; ++c) L.k1[c] = K(6, c);
     L.s1 = s7;
     L.kI1 = kI7;
+    if (kFtm && FULL && !ft) {
+      // rotation outruns absorption a hundredfold and turns (q, u) by a
+      // noticeable angle per step: try the Faraday-thick mode, whose steps
+      // follow I and V, if the transient it would carry looks small enough.
+      // The estimate needs no evaluation: this step's last one gives the
+      // rotating-frame source e^{-i chi} S = (q, u)' + k_I (q, u), so the
+      // quasi-static value and the transient d = (q, u) - e^{-i chi} S / lambda
+      // follow, and |d| k_I / |lambda| stands in for the left-out coupling
+      // (k_Q, k_C < k_I for synchrotron gas; the first evaluation in the mode
+      // checks the entry with the coefficients themselves).
+      const float kF = L.k1[NK - 1];
+      if (L.ft_cool) L.ft_cool--;
+      else if (fabsf(kF) >= kFtRatio * kI7 && fabsf(kF) * h >= 0.01f) {
+        const float sr = fmaf(kI7, L.x[1], L.k1[1]), si = fmaf(kI7, L.x[2], L.k1[2]);
+        const float il = __fdividef(1.f, fmaf(kI7, kI7, kF * kF));  // an estimate: the fast reciprocal will do
+        const float dq = L.x[1] - fmaf(sr, kI7, -si * kF) * il, du = L.x[2] - fmaf(sr, kF, si * kI7) * il;
+        const float tol = ft_tolerance(L.x[0], rtol, atol);
+        if (kI7 * kI7 * il * fmaf(dq, dq, du * du) <= tol * tol) {
+          L.ft = 1;
+          L.init = false;
+          L.ft_back = 0;
+        } else {
+          // back off: 16, 32, 64, 128, then 255 steps between estimates
+          L.ft_cool = (uint8_t)min(255, kFtRetry << L.ft_back);
+          if (L.ft_back < 4) L.ft_back++;
+        }
+      }
+    }
     return;
   }
 
@@ -1682,7 +1861,12 @@ constexpr int kDeepIquvPerSm = 2;
 }  // namespace
 }  // namespace jsh
 
-cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int schedule, bool full,
+#if JSH_FARADAY_THICK_BUILD
+#define JSH_LAUNCH_TRANSFER_MIXED jsh_launch_transfer_mixed_ft
+#else
+#define JSH_LAUNCH_TRANSFER_MIXED jsh_launch_transfer_mixed
+#endif
+cudaError_t JSH_LAUNCH_TRANSFER_MIXED(const JshRequest* d_reqs, int n_req, int schedule, bool full,
                                       uint64_t max_items, uint64_t max_hits, const JshLaunchShape& shape,
                                       unsigned int* queue, int num_sms, cudaStream_t stream) {
   if (schedule == JSH_SCHED_STATIC) {
@@ -1801,6 +1985,7 @@ cudaError_t jsh_launch_transfer_mixed(const JshRequest* d_reqs, int n_req, int s
   return cudaGetLastError();
 }
 
+#if !JSH_FARADAY_THICK_BUILD  // the host functions below are built once
 int jsh_queue64_occupancy(int block_size);
 
 int jsh_persistent_occupancy(int precision, bool full, int block_size, bool compact, bool single) {
@@ -1945,3 +2130,4 @@ int jsh_prepare_mixed(JshRequest* req, const double* nu_host, JshFreqConst* fc) 
   }
   return JSH_OK;
 }
+#endif  // !JSH_FARADAY_THICK_BUILD
