@@ -127,7 +127,8 @@ struct Slot {
   char* dev = nullptr;       // device control block: SlotHost image + counters region
   size_t counters_off = 0, counters_bytes = 0;
   // [output kind: I-only, full Stokes][kernels: general, fused benchmark family]
-  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  // [default kernels, Faraday-thick mode (full Stokes only; captured on first use)]
+  cudaGraphExec_t graph[2][2][2] = {};
   bool busy = false;
   std::vector<Request*> batch;
   int n_req = 0;
@@ -225,7 +226,7 @@ void bind_empty(Slot& sl, int i) {
 }
 
 // Enqueue (or capture) the launch sequence of slot `sl` for `n_req` records.
-cudaError_t enqueue_slot(jsh_server* S, Slot& sl, int n_req, bool full, bool fused) {
+cudaError_t enqueue_slot(jsh_server* S, Slot& sl, int n_req, bool full, bool fused, bool ft) {
   cudaStream_t st = sl.stream;
   const JshRequest* d_recs = (const JshRequest*)sl.dev;
   cudaError_t e = cudaMemcpyAsync(sl.dev, sl.host, sizeof(SlotHost), cudaMemcpyHostToDevice, st);
@@ -238,6 +239,7 @@ cudaError_t enqueue_slot(jsh_server* S, Slot& sl, int n_req, bool full, bool fus
   if (e != cudaSuccess) return e;
   JshLaunchShape shape = S->ctx->shape;
   shape.fused = fused ? 1 : 0;
+  shape.faraday_thick = ft ? 1 : 0;
   unsigned int* queue = (unsigned int*)(sl.dev + sl.counters_off + sl.counters_bytes - 256);
   e = jsh_launch_transfer(d_recs, n_req, S->cfg.precision, JSH_SCHED_PERSISTENT, full,
                           S->cap_pix * (uint64_t)S->cap_nu * (uint64_t)n_req, S->cap_pix, shape, queue,
@@ -254,15 +256,15 @@ namespace {
 // Capture the launch sequence of slot `sl` for one output kind into a graph.
 // The records are read from the control block when the graph runs, so one
 // graph per (slot, output kind) serves every batch.
-cudaError_t build_graph(jsh_server* S, Slot& sl, bool full, bool fused) {
+cudaError_t build_graph(jsh_server* S, Slot& sl, bool full, bool fused, bool ft = false) {
   cudaGraph_t g;
   cudaError_t e = cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
-  e = enqueue_slot(S, sl, S->cfg.max_batch_requests, full, fused);
+  e = enqueue_slot(S, sl, S->cfg.max_batch_requests, full, fused, ft);
   cudaError_t e2 = cudaStreamEndCapture(sl.stream, &g);
   if (e != cudaSuccess) return e;
   if (e2 != cudaSuccess) return e2;
-  e = cudaGraphInstantiate(&sl.graph[full ? 1 : 0][fused ? 1 : 0], g, 0);
+  e = cudaGraphInstantiate(&sl.graph[full ? 1 : 0][fused ? 1 : 0][ft ? 1 : 0], g, 0);
   cudaGraphDestroy(g);
   return e;
 }
@@ -278,11 +280,18 @@ int launch_batch(jsh_server* S, Slot& sl) {
   bool fused = S->cfg.precision == JSH_PREC_MIXED;
   for (int i = 0; i < n && fused; ++i)
     fused = sl.batch[i]->rec.mix.helical_log && !(sl.batch[i]->params.flags & JSH_FLAG_GENERAL_KERNELS);
-  cudaError_t e;
-  if (S->cfg.use_graphs)
-    e = cudaGraphLaunch(sl.graph[full ? 1 : 0][fused ? 1 : 0], sl.stream);
-  else
-    e = enqueue_slot(S, sl, cap, full, fused);
+  // a batch holds requests of one kind only: with or without the
+  // Faraday-thick mode (full Stokes, mixed precision)
+  const bool ft = full && S->cfg.precision == JSH_PREC_MIXED &&
+                  (sl.batch[0]->params.flags & JSH_FLAG_FARADAY_THICK) != 0;
+  cudaError_t e = cudaSuccess;
+  if (S->cfg.use_graphs) {
+    cudaGraphExec_t& gx = sl.graph[full ? 1 : 0][fused ? 1 : 0][ft ? 1 : 0];
+    if (!gx) e = build_graph(S, sl, full, fused, ft);  // the mode's graphs: on first use (the slot is idle)
+    if (e == cudaSuccess) e = cudaGraphLaunch(gx, sl.stream);
+  } else {
+    e = enqueue_slot(S, sl, cap, full, fused, ft);
+  }
   if (e != cudaSuccess) goto fail;
   e = cudaEventRecord(sl.done, sl.stream);
   if (e != cudaSuccess) goto fail;
@@ -334,13 +343,14 @@ void worker_loop(jsh_server* S) {
     for (auto& sl : S->slots) {
       if (sl.busy || S->queue.empty()) continue;
       int out_kind = S->queue.front()->params.output;
+      const int ft_kind = S->queue.front()->params.flags & JSH_FLAG_FARADAY_THICK;
       while (!S->queue.empty() && (int)sl.batch.size() < S->cfg.max_batch_requests) {
         Request* q = S->queue.front();
         if (q->state == RQ_CANCELLED) {
           S->queue.pop_front();
           continue;
         }
-        if (q->params.output != out_kind) break;
+        if (q->params.output != out_kind || (q->params.flags & JSH_FLAG_FARADAY_THICK) != ft_kind) break;
         size_t off;
         if (!S->arena.alloc(q->arena_bytes, &off)) break;  // wait for memory to free up
         q->arena_off = off;
@@ -456,9 +466,10 @@ extern "C" void jsh_server_destroy(jsh_server* S) {
   cudaSetDevice(S->ctx->device);
   for (auto& sl : S->slots) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
-    for (auto& row : sl.graph)
-      for (auto g : row)
-        if (g) cudaGraphExecDestroy(g);
+    for (auto& plane : sl.graph)
+      for (auto& row : plane)
+        for (auto g : row)
+          if (g) cudaGraphExecDestroy(g);
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.stream) cudaStreamDestroy(sl.stream);
     if (sl.host) cudaFreeHost(sl.host);

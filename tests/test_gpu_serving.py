@@ -2,7 +2,9 @@
 
 * each result is the same rendered alone and in a mix of concurrent
   requests of different sizes and frequency counts (bitwise: an item's
-  arithmetic does not depend on which batch, warp or lane runs it);
+  arithmetic does not depend on which batch, warp or lane runs it), also
+  when some requests ask for the Faraday-thick mode (their batches run its
+  kernels, the others' the default ones);
 * a budget that admits only a few requests at a time still completes every
   request (admission waits for memory to free up);
 * a request larger than the whole budget is rejected at submission;
@@ -46,6 +48,24 @@ def test_alone_equals_in_mix(ctx):
         ids = [srv.submit(j.desc(), pl.desc(), nu, p) for j, pl, nu in reqs]
         mixed = [srv.wait(i)[0] for i in ids]
     for a, m in zip(alone, mixed):
+        assert_same(a, m)
+
+
+def test_faraday_thick_requests_alone_equal_in_mix(ctx):
+    jet2, plane2, nu2, _ = W.parabolic_c2(scale=4)  # 256x256: Faraday-thick core rays
+    reqs = small_requests(4, seed=11)
+    p = J.make_params(precision="mixed", schedule="persistent", **PARAMS)
+    p_ft = J.make_params(precision="mixed", schedule="persistent", flags=A.FLAG_FARADAY_THICK, **PARAMS)
+    mix = [(jet2, plane2, nu2, p_ft), (reqs[0][0], reqs[0][1], reqs[0][2], p), (jet2, plane2, nu2, p),
+           (reqs[1][0], reqs[1][1], reqs[1][2], p_ft), (reqs[2][0], reqs[2][1], reqs[2][2], p),
+           (reqs[3][0], reqs[3][1], reqs[3][2], p_ft)]
+    alone = [ctx.render(j.desc(), pl.desc(), nu, q) for j, pl, nu, q in mix]
+    # the mode engages on the ParabaloidCone core: fewer evaluations than the default kernels
+    assert alone[0][1]["rhs_evals"] < alone[2][1]["rhs_evals"]
+    with S.Server(ctx, max_inflight_batches=2, max_batch_requests=8) as srv:
+        ids = [srv.submit(j.desc(), pl.desc(), nu, q) for j, pl, nu, q in mix]
+        mixed = [srv.wait(i, timeout_ms=120000)[0] for i in ids]
+    for (a, _), m in zip(alone, mixed):
         assert_same(a, m)
 
 
