@@ -319,17 +319,21 @@ def faraday_depth(jet, plane, nu_hz, pix, n_pts=4000):
     return total
 
 
-def serving_leg(ctx, n_requests, rate_hz=200.0, warm=True):
+def serving_leg(ctx, n_requests, rate_hz=200.0, warm=True, flags=0):
     """Replay the seeded Poisson request stream (priors of the model-fitting
     sweep) through the serving loop in real time; latency is arrival to
-    result on the host."""
+    result on the host.  ``flags``: JSH_FLAG_* of every request."""
+    from jetshow_gb300 import jet as J
     from jetshow_gb300 import serving as S
+    from jetshow_gb300 import workloads as W
     stream = S.request_stream(n_requests, rate_hz=rate_hz, seed=42)
+    params = J.make_params(precision="mixed", schedule="persistent", flags=flags, **W.ACCURATE_KW)
     counts = {}
     with S.Server(ctx, max_inflight_batches=3, max_batch_requests=16) as srv:
         if warm:  # one short stream first: pages in the result path and the host threads
-            S.run_stream(srv, [r for r in S.request_stream(8, rate_hz=200.0, seed=7) if r.size_label == "64x64"])
-        records, wall = S.run_stream(srv, stream, counts=counts)
+            S.run_stream(srv, [r for r in S.request_stream(8, rate_hz=200.0, seed=7) if r.size_label == "64x64"],
+                         params=params)
+        records, wall = S.run_stream(srv, stream, params=params, counts=counts)
     lat = np.array([r["latency_ms"] for r in records])
     queue = np.array([r["queue_ms"] for r in records])
     items = sum(r["n_items"] for r in records)
@@ -625,13 +629,18 @@ def main():
                        "tau_evals_per_step": int(n_tau), "iquv_evals_per_step": int(n_iquv)},
             "fp64_peak_tflops": peaks["fp64_tflops"]}
     cpu = cpu_baseline_sample(jet, plane, nu, kw) if rank == 0 and conical else None
-    serving = saturated = sustained = None
+    serving = saturated = sustained = sustained_ft = None
     if args.serve_requests > 0:
         serving = serving_leg(ctx, args.serve_requests)
         if args.saturate_rate > 0:
             saturated = serving_leg(ctx, args.serve_requests, rate_hz=args.saturate_rate, warm=False)
         if args.sustain_rate > 0 and args.sustain_requests > 0:
             sustained = serving_leg(ctx, args.sustain_requests, rate_hz=args.sustain_rate, warm=False)
+            try:  # the same stream, every request with the Faraday-thick mode
+                sustained_ft = serving_leg(ctx, args.sustain_requests, rate_hz=args.sustain_rate, warm=False,
+                                           flags=A.FLAG_FARADAY_THICK)
+            except Exception as e:  # reported, never fatal to the bench line
+                sustained_ft = {"error": f"{type(e).__name__}: {e}"}
     gridded = gridded_leg(ctx) if args.gridded else None
     configs = None
     if args.configs and conical and rank == 0:
@@ -657,7 +666,8 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": float(np.mean(e2e_ms))},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
-                "serving_saturated": saturated, "serving_sustainable": sustained, "gridded": gridded,
+                "serving_saturated": saturated, "serving_sustainable": sustained,
+                "serving_sustainable_faraday_thick": sustained_ft, "gridded": gridded,
                 "configs": configs,
                 "gpu_launches": int(st_b["kernels_launched"]) * args.steps,
                 "gpu_launches_per_step": ({"plane": 2, "hit": 1, "rank": 3, "tau": 2, "iquv_rank": 6, "iquv": 2}
