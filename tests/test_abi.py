@@ -90,3 +90,22 @@ def test_tau_panel_rule_is_gauss_kronrod(lib):
     gx, gw = np.polynomial.legendre.leggauss(7)
     assert np.allclose(x[1::2], gx, rtol=0, atol=1e-15) and np.allclose(wg[1::2], gw, rtol=0, atol=1e-15)
     assert np.all(wg[0::2] == 0)
+
+
+def test_faraday_thick_build_is_linked_and_uncontracted(lib):
+    """The Faraday-thick mode's kernels are jsh_persistent.cu compiled a
+    second time (jsh_persistent_ft.cu): that unit is built, like its twin,
+    without compiler-fused multiply-adds (every form of the mixed path gives
+    the same bits only then), rebuilt when its twin changes, and its launch
+    sequence is linked beside the default one."""
+    from jetshow_gb300 import build as B
+    assert "jsh_persistent_ft.cu" in B.CU_SOURCES
+    assert {"jsh_persistent.cu", "jsh_persistent_ft.cu"} <= B.NO_CONTRACT
+    assert B.INCLUDED["jsh_persistent_ft.cu"] == ["jsh_persistent.cu"]
+    src = open(os.path.join(REPO, "jetshow_gb300", "csrc", "jsh_persistent_ft.cu")).read()
+    assert "#define JSH_FARADAY_THICK_BUILD 1" in src and '#include "jsh_persistent.cu"' in src
+    import subprocess
+    syms = subprocess.run(["nm", "-D", A.LIB_PATH], capture_output=True, text=True).stdout
+    assert "28jsh_launch_transfer_mixed_ftP" in syms  # the mode's launch sequence (mangled name)
+    assert "25jsh_launch_transfer_mixedP" in syms  # the default one
+    assert A.FLAG_FARADAY_THICK == 0x100
